@@ -1,0 +1,224 @@
+"""faces_gb300 -- GB300 (sm_103a) Faces halo-sum step behind the reference's
+Faces interface.
+
+The reference's in-process API is ``class Faces { Faces(rank, lx, ly, lz, mx,
+my, mz, n); void share(Double6D &u, bool compute = true); }``
+(gpu/v-26-messages/Faces.h:6-39) with the field a DArray<double,6>
+(gpu/DArray.h).  :class:`Faces` here is that object for all lx*ly*lz virtual
+ranks of one GPU; the field is a CUDA float64 tensor (or raw device pointer)
+in the DArray layout, ranks stored rank-major.  Every call goes through the C
+ABI of include/faces_gb300.h in ``lib/libfaces_gb300.so``; there is no CPU
+fallback -- importing this package without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+__all__ = ["Faces", "FacesError", "lib", "library_path", "PERIODIC", "MESSAGES", "GATHER"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(HERE, "lib", "libfaces_gb300.so")
+exe_path = os.path.join(HERE, "bin", "faces")
+
+PERIODIC = 0x1
+MESSAGES = 0x2
+GATHER = 0x4
+
+_ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
+
+
+class FacesError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"faces_gb300 error {code} ({_ERRNAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(library_path):
+        raise ImportError(
+            f"{library_path} is missing: build it with `python -m faces_gb300.build` "
+            "(faces_gb300 has no CPU fallback)")
+    L = ctypes.CDLL(library_path)
+    c_int, c_long, c_uint, c_ull, vp = ctypes.c_int, ctypes.c_long, ctypes.c_uint, ctypes.c_ulonglong, ctypes.c_void_p
+    dp = ctypes.c_void_p
+    L.faces_create.argtypes = [ctypes.POINTER(vp)] + [c_int] * 7 + [c_uint]
+    L.faces_destroy.argtypes = [vp]
+    L.faces_layout.argtypes = [vp, ctypes.POINTER(c_long), ctypes.POINTER(c_long), ctypes.POINTER(c_long)]
+    L.faces_field_alloc.argtypes = [vp, ctypes.POINTER(vp)]
+    L.faces_field_free.argtypes = [vp]
+    L.faces_share.argtypes = [vp, dp, c_int, vp]
+    L.faces_share_n.argtypes = [vp, dp, c_int, c_int, vp]
+    L.faces_init_ref.argtypes = [vp, dp, vp]
+    L.faces_init_int.argtypes = [vp, dp, c_ull, vp]
+    L.faces_check.argtypes = [vp, dp, c_int, c_ull, c_int, c_int, ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                              ctypes.POINTER(ctypes.c_double), vp]
+    L.faces_run_host.argtypes = [vp, dp, dp, c_int, c_int, vp]
+    L.faces_set_tuning.argtypes = [vp, c_int, c_int]
+    L.faces_launches_per_share.argtypes = [vp, c_int]
+    L.faces_last_error.restype = ctypes.c_char_p
+    for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
+                 "faces_share", "faces_share_n", "faces_init_ref", "faces_init_int", "faces_check",
+                 "faces_run_host", "faces_set_tuning", "faces_launches_per_share"):
+        getattr(L, name).restype = c_int
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> int:
+    if rc < 0:
+        raise FacesError(rc, lib().faces_last_error().decode(errors="replace"))
+    return rc
+
+
+def _ptr(u) -> int:
+    """Device address of a CUDA tensor (float64, contiguous) or an int."""
+    if isinstance(u, int):
+        return u
+    import torch
+    if not isinstance(u, torch.Tensor):
+        raise TypeError("field must be a torch CUDA tensor or a device address")
+    if not u.is_cuda or u.dtype != torch.float64 or not u.is_contiguous():
+        raise ValueError("field must be a contiguous float64 CUDA tensor")
+    return u.data_ptr()
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available() and torch.cuda.is_initialized():
+                return torch.cuda.current_stream().cuda_stream
+        except Exception:
+            pass
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+@dataclass(frozen=True)
+class CheckResult:
+    maxrel: float
+    npass: int
+    rank_maxrel: list
+    where: tuple  # rank, ix, iy, iz, jx, jy, jz of the largest error
+    values: tuple  # (u, expected) there
+
+    @property
+    def passed(self) -> bool:
+        return self.maxrel < 1e-15
+
+
+class Faces:
+    """All lx*ly*lz ranks' Faces objects (gpu/v-26-messages/Faces.cc:10-82).
+
+    periodic -- wrap the rank grid (the reference never wraps, K1)
+    messages -- v-26 strategy: 26 messages per rank packed, swapped by buffer
+                direction and unpack-added (else one owner per shared point)
+    gather   -- force the generic one-thread-per-point kernel
+    """
+
+    def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
+                 periodic: bool = False, messages: bool = False, gather: bool = False):
+        flags = (PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
+        h = ctypes.c_void_p()
+        _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
+        self._h = h
+        self.shape = (lx, ly, lz, mx, my, mz, n)
+        self.periodic, self.messages, self.gather = periodic, messages, gather
+        s = (ctypes.c_long * 6)()
+        rd, tot = ctypes.c_long(), ctypes.c_long()
+        _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
+        self.strides = tuple(s)
+        self.rank_doubles = rd.value
+        self.total_doubles = tot.value
+        self.nranks = lx * ly * lz
+
+    # -- lifetime -------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().faces_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- geometry ---------------------------------------------------------
+    @property
+    def points(self) -> int:
+        lx, ly, lz, mx, my, mz, n = self.shape
+        return n ** 3 * mx * my * mz * lx * ly * lz
+
+    def index(self, ix, iy, iz, jx, jy, jz, rank: int = 0) -> int:
+        """DArray index (gpu/DArray.h:34-38) of a point of one rank."""
+        s = self.strides
+        return rank * self.rank_doubles + ix + iy * s[1] + iz * s[2] + jx * s[3] + jy * s[4] + jz * s[5]
+
+    def field(self, device=None):
+        """A zero-filled CUDA float64 tensor of the field size (DArray alloc)."""
+        import torch
+        return torch.zeros(self.total_doubles, dtype=torch.float64, device=device or "cuda")
+
+    # -- the step ---------------------------------------------------------
+    def share(self, u, compute: bool = True, stream=None) -> None:
+        """Faces::share(u, compute) on every rank (stream-ordered)."""
+        _check(lib().faces_share(self._h, _ptr(u), int(compute), _stream(stream)))
+
+    def share_n(self, u, nshares: int, compute: bool = True, stream=None) -> None:
+        _check(lib().faces_share_n(self._h, _ptr(u), int(compute), nshares, _stream(stream)))
+
+    def init_ref(self, u, stream=None) -> None:
+        """gpu/main.cc:10-19 initial values on every rank."""
+        _check(lib().faces_init_ref(self._h, _ptr(u), _stream(stream)))
+
+    def init_int(self, u, seed: int, stream=None) -> None:
+        """Integer-valued doubles uniform in [0,2^20)."""
+        _check(lib().faces_init_int(self._h, _ptr(u), ctypes.c_ulonglong(seed), _stream(stream)))
+
+    def check(self, u, *, init: str = "ref", seed: int = 0, nshares: int = 1, compute: bool = True,
+              stream=None) -> CheckResult:
+        """gpu/main.cc:39-105 on the device against the closed form of nshares shares."""
+        rm = (ctypes.c_double * self.nranks)()
+        mx = ctypes.c_double()
+        npass = ctypes.c_int()
+        where = (ctypes.c_int * 7)()
+        vals = (ctypes.c_double * 2)()
+        _check(lib().faces_check(self._h, _ptr(u), 0 if init == "ref" else 1, ctypes.c_ulonglong(seed), nshares,
+                                 int(compute), rm, ctypes.byref(mx), ctypes.byref(npass), where, vals,
+                                 _stream(stream)))
+        return CheckResult(mx.value, npass.value, list(rm), tuple(where), tuple(vals))
+
+    def run_host(self, u_in, u_out, nshares: int, compute: bool = True, stream=None) -> None:
+        """End to end from host memory: upload, nshares shares, download."""
+        import numpy as np
+        for a in (u_in, u_out):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                    and a.size == self.total_doubles):
+                raise ValueError("host buffers must be contiguous float64 arrays of the field size")
+        _check(lib().faces_run_host(self._h, u_in.ctypes.data, u_out.ctypes.data, int(compute), nshares,
+                                    _stream(stream)))
+
+    def set_tuning(self, chunk: int = 0, tiles_per_block: int = 0) -> None:
+        _check(lib().faces_set_tuning(self._h, chunk, tiles_per_block))
+
+    def launches_per_share(self, compute: bool = True) -> int:
+        return _check(lib().faces_launches_per_share(self._h, int(compute)))

@@ -1,0 +1,353 @@
+// faces_api.cu -- the C ABI of include/faces_gb300.h.
+//
+// Host side of the reference's Faces class (gpu/v-26-messages/Faces.cc:10-103)
+// for lx*ly*lz virtual ranks at once: neighbour tables, direction-keyed
+// message buffers, launch of the sm_103a kernels in kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/faces_gb300.h"
+#include "geom.cuh"
+#include "kernels.cuh"
+#include "tables.h"
+
+using namespace faces;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+  return fail(e == cudaErrorMemoryAllocation ? FACES_ENOMEM : FACES_ECUDA, "%s: %s (%s)", what,
+              cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define CUDA_TRY(call, what)                  \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+struct faces_ctx {
+  int L[3], m[3], n;
+  unsigned flags;
+  int nranks;
+  long sjy, sjz, R, total;
+  std::vector<int> nbr;       // [rank*27+dir]
+  std::vector<long> msg_off;  // [rank*27+dir], -1: none
+  long msg_total = 0;
+  int *d_nbr = nullptr;
+  long *d_off = nullptr;
+  double *d_msg = nullptr;
+  unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
+  double *d_field = nullptr;                // faces_run_host's device copy
+  int chunk = 0, tpb = 0;
+  RowPlan plan;
+
+  FieldDesc desc(double *u) const
+  {
+    FieldDesc f;
+    f.u = u;
+    f.sjy = sjy; f.sjz = sjz; f.R = R;
+    f.n = n;
+    for (int a = 0; a < 3; a++) { f.m[a] = m[a]; f.L[a] = L[a]; }
+    f.periodic = (flags & FACES_PERIODIC) ? 1 : 0;
+    f.mode = (flags & FACES_MESSAGES) ? kMessages : kDirect;
+    f.nranks = nranks;
+    f.msg = d_msg;
+    f.msg_off = d_off;
+    f.nbr = d_nbr;
+    return f;
+  }
+};
+
+namespace {
+
+// default x-chunk: whole rows when that already fills the GPU, else split
+// rows until about 150k threads are resident
+int default_chunk(const faces_ctx &c)
+{
+  const bool virt = (c.flags & FACES_MESSAGES) || !(c.flags & FACES_PERIODIC);
+  const long rows = (long)c.nranks * (c.m[1] + virt) * (c.m[2] + virt);
+  const int P = c.n <= 2 ? 2 : c.n <= 4 ? 4 : c.n <= 8 ? 8 : 16;
+  const long tt = ((P * c.n + 31) / 32) * 32;
+  const long want = 152L * 1024;
+  long nch = (want + rows * tt - 1) / (rows * tt);
+  if (nch < 1) nch = 1;
+  if (nch > c.m[0]) nch = c.m[0];
+  return (int)((c.m[0] + nch - 1) / nch);
+}
+
+void replan(faces_ctx &c)
+{
+  const FieldDesc f = c.desc(nullptr);
+  c.plan = make_row_plan(f, c.chunk > 0 ? c.chunk : default_chunk(c), c.tpb);
+}
+
+int check_ctx(const faces_ctx *c)
+{
+  if (!c) return fail(FACES_EINVAL, "null context");
+  return FACES_OK;
+}
+
+int check_field(const double *u)
+{
+  if (!u) return fail(FACES_EINVAL, "null field pointer");
+  if (!aligned16(u)) return fail(FACES_EALIGN, "field pointer %p is not 16-byte aligned", (const void *)u);
+  return FACES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *faces_last_error(void) { return g_err.c_str(); }
+
+int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags)
+{
+  if (!out) return fail(FACES_EINVAL, "null output pointer");
+  *out = nullptr;
+  if (lx < 1 || ly < 1 || lz < 1) return fail(FACES_EINVAL, "rank grid %d x %d x %d must be positive", lx, ly, lz);
+  if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
+  if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
+  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER)) return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
+  const long nranks = (long)lx * ly * lz;
+  if (nranks > 65535 / 27) return fail(FACES_EINVAL, "%ld ranks: at most %d virtual ranks", nranks, 65535 / 27);
+  faces_ctx *c = new (std::nothrow) faces_ctx();
+  if (!c) return fail(FACES_ENOMEM, "host allocation failed");
+  c->L[0] = lx; c->L[1] = ly; c->L[2] = lz;
+  c->m[0] = mx; c->m[1] = my; c->m[2] = mz;
+  c->n = n;
+  c->flags = flags;
+  c->nranks = (int)nranks;
+  c->sjy = (long)n * n * n * mx;
+  c->sjz = jz_stride(n, mx, my);
+  c->R = c->sjz * mz;
+  c->total = c->R * nranks;
+  c->nbr = neighbour_table(c->L, (flags & FACES_PERIODIC) != 0);
+  c->msg_off.assign(nranks * 27, -1);
+  if (flags & FACES_MESSAGES) c->msg_total = message_offsets(c->desc(nullptr), c->nbr, c->msg_off);
+  cudaError_t e;
+  if ((e = cudaMalloc(&c->d_nbr, sizeof(int) * nranks * 27)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_off, sizeof(long) * nranks * 27)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_scratch, sizeof(unsigned long long) * (nranks + 4))) != cudaSuccess ||
+      (c->msg_total > 0 && (e = cudaMalloc(&c->d_msg, sizeof(double) * c->msg_total)) != cudaSuccess)) {
+    faces_destroy(c);
+    return cuda_fail(e, "faces_create: device allocation");
+  }
+  if ((e = cudaMemcpy(c->d_nbr, c->nbr.data(), sizeof(int) * nranks * 27, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(c->d_off, c->msg_off.data(), sizeof(long) * nranks * 27, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (c->d_msg && (e = cudaMemset(c->d_msg, 0, sizeof(double) * c->msg_total)) != cudaSuccess)) {
+    faces_destroy(c);
+    return cuda_fail(e, "faces_create: upload");
+  }
+  replan(*c);
+  *out = c;
+  return FACES_OK;
+}
+
+int faces_destroy(faces_ctx *c)
+{
+  if (!c) return FACES_OK;
+  cudaFree(c->d_nbr);
+  cudaFree(c->d_off);
+  cudaFree(c->d_msg);
+  cudaFree(c->d_scratch);
+  cudaFree(c->d_field);
+  delete c;
+  return FACES_OK;
+}
+
+int faces_layout(const faces_ctx *c, long strides[6], long *rank_doubles, long *total_doubles)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (strides) {
+    const long n = c->n;
+    strides[0] = 1;
+    strides[1] = n;
+    strides[2] = n * n;
+    strides[3] = n * n * n;
+    strides[4] = c->sjy;
+    strides[5] = c->sjz;
+  }
+  if (rank_doubles) *rank_doubles = c->R;
+  if (total_doubles) *total_doubles = c->total;
+  return FACES_OK;
+}
+
+int faces_field_alloc(const faces_ctx *c, double **u)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (!u) return fail(FACES_EINVAL, "null output pointer");
+  *u = nullptr;
+  CUDA_TRY(cudaMalloc(u, sizeof(double) * c->total), "faces_field_alloc");
+  CUDA_TRY(cudaMemset(*u, 0, sizeof(double) * c->total), "faces_field_alloc: memset");
+  return FACES_OK;
+}
+
+int faces_field_free(double *u)
+{
+  CUDA_TRY(cudaFree(u), "faces_field_free");
+  return FACES_OK;
+}
+
+int faces_set_tuning(faces_ctx *c, int chunk, int tiles_per_block)
+{
+  if (int rc = check_ctx(c)) return rc;
+  c->chunk = chunk > 0 ? chunk : 0;
+  c->tpb = tiles_per_block > 0 ? tiles_per_block : 0;
+  replan(*c);
+  return FACES_OK;
+}
+
+int faces_launches_per_share(const faces_ctx *c, int compute)
+{
+  if (int rc = check_ctx(c)) return rc;
+  (void)compute;
+  return (c->flags & FACES_MESSAGES) ? 2 : 1;
+}
+
+static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
+{
+  const FieldDesc f = c->desc(u);
+  if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
+  if (compute && !(c->flags & FACES_GATHER) && row_kernel_supported(c->n))
+    CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
+  else
+    CUDA_TRY(launch_gather(f, compute, s), "gather kernel launch");
+  return FACES_OK;
+}
+
+int faces_share(faces_ctx *c, double *u, int compute, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (int rc = check_field(u)) return rc;
+  return share_once(c, u, compute, static_cast<cudaStream_t>(stream));
+}
+
+int faces_share_n(faces_ctx *c, double *u, int compute, int nshares, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (int rc = check_field(u)) return rc;
+  if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
+  for (int i = 0; i < nshares; i++)
+    if (int rc = share_once(c, u, compute, static_cast<cudaStream_t>(stream))) return rc;
+  return FACES_OK;
+}
+
+int faces_init_ref(faces_ctx *c, double *u, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (int rc = check_field(u)) return rc;
+  CUDA_TRY(launch_init_ref(c->desc(u), static_cast<cudaStream_t>(stream)), "init kernel launch");
+  return FACES_OK;
+}
+
+int faces_init_int(faces_ctx *c, double *u, unsigned long long seed, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (int rc = check_field(u)) return rc;
+  CUDA_TRY(launch_init_int(c->desc(u), seed, static_cast<cudaStream_t>(stream)), "init kernel launch");
+  return FACES_OK;
+}
+
+int faces_check(faces_ctx *c, const double *u, int init, unsigned long long seed, int nshares, int compute,
+                double *rank_maxrel, double *maxrel, int *npass, int where[7], double vals[2], void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (int rc = check_field(u)) return rc;
+  if (init != 0 && init != 1) return fail(FACES_EINVAL, "init = %d: 0 (reference formula) or 1 (integer seed)", init);
+  if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int R = c->nranks;
+  unsigned long long *rank_max = c->d_scratch, *gmax = c->d_scratch + R, *first = c->d_scratch + R + 1;
+  double *dvals = reinterpret_cast<double *>(c->d_scratch + R + 2);
+  const FieldDesc f = c->desc(const_cast<double *>(u));
+  CUDA_TRY(cudaMemsetAsync(c->d_scratch, 0, sizeof(unsigned long long) * (R + 1), s), "check: clear");
+  CUDA_TRY(cudaMemsetAsync(first, 0xff, sizeof(unsigned long long), s), "check: clear");
+  CUDA_TRY(launch_check(f, init, seed, nshares, compute, rank_max, gmax, 0, first, -1, dvals, s), "check kernel");
+  std::vector<unsigned long long> h(R + 1);
+  CUDA_TRY(cudaMemcpyAsync(h.data(), c->d_scratch, sizeof(unsigned long long) * (R + 1), cudaMemcpyDeviceToHost, s),
+           "check: read back");
+  CUDA_TRY(cudaStreamSynchronize(s), "check: synchronize");
+  int pass = 0;
+  for (int r = 0; r < R; r++) {
+    double d;
+    std::memcpy(&d, &h[r], sizeof(d));
+    if (rank_maxrel) rank_maxrel[r] = d;
+    if (d < 1e-15) pass++;
+  }
+  double g;
+  std::memcpy(&g, &h[R], sizeof(g));
+  if (maxrel) *maxrel = g;
+  if (npass) *npass = pass;
+  if (where || vals) {
+    long p = 0;
+    if (h[R] != 0) {
+      CUDA_TRY(launch_check(f, init, seed, nshares, compute, rank_max, gmax, h[R], first, -1, dvals, s), "check: locate");
+      unsigned long long hp;
+      CUDA_TRY(cudaMemcpyAsync(&hp, first, sizeof(hp), cudaMemcpyDeviceToHost, s), "check: read back");
+      CUDA_TRY(cudaStreamSynchronize(s), "check: synchronize");
+      p = (long)hp;
+    }
+    const long n = c->n;
+    const long per_rank = n * n * n * c->m[0] * c->m[1] * c->m[2];
+    if (where) {
+      long t = p % per_rank;
+      where[0] = (int)(p / per_rank);
+      where[1] = (int)(t % n); t /= n;
+      where[2] = (int)(t % n); t /= n;
+      where[3] = (int)(t % n); t /= n;
+      where[4] = (int)(t % c->m[0]); t /= c->m[0];
+      where[5] = (int)(t % c->m[1]); t /= c->m[1];
+      where[6] = (int)t;
+    }
+    if (vals) {
+      CUDA_TRY(launch_check(f, init, seed, nshares, compute, rank_max, gmax, 0, first, p, dvals, s), "check: values");
+      CUDA_TRY(cudaMemcpyAsync(vals, dvals, 2 * sizeof(double), cudaMemcpyDeviceToHost, s), "check: read back");
+      CUDA_TRY(cudaStreamSynchronize(s), "check: synchronize");
+    }
+  }
+  return FACES_OK;
+}
+
+int faces_run_host(faces_ctx *c, const double *u_in, double *u_out, int compute, int nshares, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (!u_in || !u_out) return fail(FACES_EINVAL, "null host buffer");
+  if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!c->d_field) CUDA_TRY(cudaMalloc(&c->d_field, sizeof(double) * c->total), "faces_run_host: device field");
+  const size_t bytes = sizeof(double) * c->total;
+  CUDA_TRY(cudaMemcpyAsync(c->d_field, u_in, bytes, cudaMemcpyHostToDevice, s), "faces_run_host: upload");
+  if (int rc = faces_share_n(c, c->d_field, compute, nshares, stream)) return rc;
+  CUDA_TRY(cudaMemcpyAsync(u_out, c->d_field, bytes, cudaMemcpyDeviceToHost, s), "faces_run_host: download");
+  CUDA_TRY(cudaStreamSynchronize(s), "faces_run_host: synchronize");
+  return FACES_OK;
+}
+
+}  // extern "C"

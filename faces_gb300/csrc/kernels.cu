@@ -1,0 +1,560 @@
+// kernels.cu -- sm_103a kernels of the Faces halo-sum step.
+//
+// One share makes every point that 2 (face), 4 (edge) or 8 (corner) element
+// copies hold equal to the sum of its copies, inside each rank and across the
+// 26 neighbour ranks (the reference's oracle gpu/Mugs.cc:86-416 and strategy
+// gpu/v-26-messages/Faces.cc:111-678).  Every kernel here forms that sum as
+// a tree in dimension order -- x pairs, then y pairs, then z pairs -- the
+// order Mugs's in-place passes produce (gpu/Mugs.cc:140-202), so on one rank
+// the result equals Mugs bit for bit on any input, and every copy of a point
+// receives the identical value on every rank.
+//
+// Kernels
+//   rows_kernel<N>   the step (compute=true): one thread per physical element
+//                    row, walking an x-chunk; x pairs in registers, y pairs by
+//                    warp shuffle, z pairs through shared memory.  Direct
+//                    mode (one owner per shared point, neighbours' memory read
+//                    and written in place) or message mode (v-26: remote
+//                    copies read from the 26 received messages, each rank
+//                    writes only its own copies).
+//   gather_kernel    the step for any n and compute=false: one thread per
+//                    owned shared point gathers its copies.
+//   pack_kernel      message mode: the 26 raw boundary messages of every rank
+//                    (gpu/v-26-messages/Faces.cc:243-293).
+//   init_*_kernel    gpu/main.cc:10-19 formula, or seeded integer values.
+//   check_kernel     closed-form expected values after s shares, compared
+//                    with the rule of gpu/main.cc:39-105.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "geom.cuh"
+#include "kernels.cuh"
+#include "rows_setup.cuh"
+
+namespace faces {
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x)
+{
+  // Steele, Lea & Flood, "Fast splittable pseudorandom number generators"
+  uint64_t z = x + 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double int_value(uint64_t seed, long index)
+{
+  return (double)(splitmix64(seed * 0x9E3779B97F4A7C15ULL + (uint64_t)index) >> 44);
+}
+
+// gpu/main.cc:18 with every multiply and add rounded separately (no FMA
+// contraction), so the device and the host formula agree bit for bit
+__device__ __forceinline__ double ref_value(int ix, int iy, int iz, int jx, int jy, int jz)
+{
+  const int whole = jz * 10000 + jy * 100 + jx;
+  double v = __dadd_rn((double)whole, __dmul_rn((double)iz, 0.01));
+  v = __dadd_rn(v, __dmul_rn((double)iy, 0.0001));
+  v = __dadd_rn(v, __dmul_rn((double)ix, 0.000001));
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// init kernels (whole allocation: padding set to zero, as DArray's memset)
+// ---------------------------------------------------------------------------
+
+__global__ void init_ref_kernel(FieldDesc f, long total)
+{
+  const long n = f.n;
+  const long plane = f.sjy * f.m[1];
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    const long rem = p % f.R;
+    const int jz = (int)(rem / f.sjz);
+    const long q = rem % f.sjz;
+    double v = 0.0;
+    if (q < plane) {
+      const int jy = (int)(q / f.sjy);
+      long t = q % f.sjy;
+      const int jx = (int)(t / (n * n * n));
+      t %= n * n * n;
+      const int iz = (int)(t / (n * n));
+      t %= n * n;
+      v = ref_value((int)(t % n), (int)(t / n), iz, jx, jy, jz);
+    }
+    f.u[p] = v;
+  }
+}
+
+__global__ void init_int_kernel(FieldDesc f, long total, unsigned long long seed)
+{
+  const long plane = f.sjy * f.m[1];
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    const long q = (p % f.R) % f.sjz;
+    f.u[p] = (q < plane) ? int_value(seed, p) : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pack: the 26 messages of every rank, raw values before any sum
+// ---------------------------------------------------------------------------
+
+__global__ void pack_kernel(FieldDesc f)
+{
+  const int rd = blockIdx.y;  // rank*27 + dir
+  const int r = rd / 27, dir = rd % 27;
+  if (dir == 13 || f.msg_off[rd] < 0) return;
+  const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
+  const long sz = region_size(f, d);
+  double *out = f.msg + f.msg_off[rd];
+  const double *ur = f.u + (long)r * f.R;
+  const int n = f.n;
+  for (long pos = blockIdx.x * (long)blockDim.x + threadIdx.x; pos < sz; pos += (long)gridDim.x * blockDim.x) {
+    int i[3], j[3];
+    long t = pos;
+    for (int a = 0; a < 3; a++)
+      if (d[a] == 0) { i[a] = (int)(t % n); t /= n; }
+    for (int a = 0; a < 3; a++)
+      if (d[a] == 0) { j[a] = (int)(t % f.m[a]); t /= f.m[a]; }
+    for (int a = 0; a < 3; a++)
+      if (d[a] != 0) {
+        i[a] = d[a] < 0 ? 0 : n - 1;
+        j[a] = d[a] < 0 ? 0 : f.m[a] - 1;
+      }
+    out[pos] = ur[elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gather: one thread per owned shared point (any n, compute on or off)
+// ---------------------------------------------------------------------------
+
+// Rank-local point coordinate g in [0, m*(n-1)] along one axis: element E
+// holds g = E*(n-1)+i.  A point with g % (n-1) == 0 has a lower copy (E-1,
+// n-1) and an upper copy (E, 0); elements -1 and m belong to the neighbours.
+struct Copies {
+  int cnt;
+  int e[2], i[2];
+};
+
+__device__ __forceinline__ void local_axis(int g, int n, Copies &c)
+{
+  const int nm1 = n - 1, E = g / nm1, i = g % nm1;
+  if (i) { c.cnt = 1; c.e[0] = E; c.i[0] = i; return; }
+  c.cnt = 2; c.e[0] = E - 1; c.i[0] = nm1; c.e[1] = E; c.i[1] = 0;
+}
+
+__global__ void gather_kernel(FieldDesc f, int compute)
+{
+  const int n = f.n, nm1 = n - 1;
+  const long G0 = (long)f.m[0] * nm1 + 1, G1 = (long)f.m[1] * nm1 + 1, G2 = (long)f.m[2] * nm1 + 1;
+  const long per_rank = G0 * G1 * G2;
+  const long total = per_rank * f.nranks;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(p / per_rank);
+    long t = p % per_rank;
+    const int g[3] = {(int)(t % G0), (int)((t / G0) % G1), (int)(t / (G0 * G1))};
+    // a point is shared only if it lies on an element boundary somewhere
+    if (g[0] % nm1 && g[1] % nm1 && g[2] % nm1) continue;
+    bool onb = false, skip = false;
+    Copies c[3];
+    for (int a = 0; a < 3; a++) {
+      const int Ga = f.m[a] * nm1;
+      onb |= (g[a] == 0 || g[a] == Ga);
+      int up[3] = {0, 0, 0};
+      up[a] = 1;
+      // direct mode: the upper rank owns the points of the shared plane
+      if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(up[0], up[1], up[2])) >= 0) skip = true;
+      local_axis(g[a], n, c[a]);
+      // drop copies whose neighbour rank does not exist
+      int k = 0;
+      for (int b = 0; b < c[a].cnt; b++) {
+        const int e = c[a].e[b];
+        int dv[3] = {0, 0, 0};
+        dv[a] = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
+        if (dv[a] && nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) < 0) continue;
+        c[a].e[k] = e; c[a].i[k] = c[a].i[b]; k++;
+      }
+      c[a].cnt = k;
+    }
+    if (skip) continue;
+    if (c[0].cnt * c[1].cnt * c[2].cnt < 2) continue;
+    if (!compute && !onb) continue;
+    double v[2][2][2];
+    double *w[2][2][2];
+    for (int bz = 0; bz < c[2].cnt; bz++)
+      for (int by = 0; by < c[1].cnt; by++)
+        for (int bx = 0; bx < c[0].cnt; bx++) {
+          int e[3] = {c[0].e[bx], c[1].e[by], c[2].e[bz]};
+          const int i[3] = {c[0].i[bx], c[1].i[by], c[2].i[bz]};
+          int d[3], j[3];
+          for (int a = 0; a < 3; a++) {
+            d[a] = e[a] < 0 ? -1 : (e[a] >= f.m[a] ? 1 : 0);
+            j[a] = e[a] < 0 ? f.m[a] - 1 : (e[a] >= f.m[a] ? 0 : e[a]);
+          }
+          const int dir = dir_index(d[0], d[1], d[2]);
+          if (dir == 13 || f.mode == kDirect) {
+            const int q = (dir == 13) ? r : nbr_of(f, r, dir);
+            double *ptr = f.u + (long)q * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
+            w[bz][by][bx] = ptr;
+            v[bz][by][bx] = *ptr;
+          } else {
+            const double *rb = recv_of(f, r, dir);
+            w[bz][by][bx] = nullptr;
+            v[bz][by][bx] = rb[region_pos(f, d, i, j)];
+          }
+        }
+    double sy[2];
+    for (int bz = 0; bz < c[2].cnt; bz++) {
+      double sx[2];
+      for (int by = 0; by < c[1].cnt; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
+      sy[bz] = (c[1].cnt == 2) ? sx[0] + sx[1] : sx[0];
+    }
+    const double s = (c[2].cnt == 2) ? sy[0] + sy[1] : sy[0];
+    for (int bz = 0; bz < c[2].cnt; bz++)
+      for (int by = 0; by < c[1].cnt; by++)
+        for (int bx = 0; bx < c[0].cnt; bx++)
+          if (w[bz][by][bx]) *w[bz][by][bx] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// rows: the fused step (compute = true); tiles and slots in rows_setup.cuh
+// ---------------------------------------------------------------------------
+//
+// Per element the slot forms w = (seam sum, row[1..n-2]) -- the x pair
+// carry(row[n-1] of the previous element) + row[0] -- then y pairs between
+// slots (0,sz) and (n-1,sz) (same warp: shuffle), then z pairs between (sy,0)
+// and (sy,n-1) (other warps: shared memory, one named barrier per element).
+
+template <int N>
+__device__ __forceinline__ void load_row(double (&v)[N], const double *p)
+{
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < N; k += 2) {
+      const double2 t = *reinterpret_cast<const double2 *>(p + k);
+      v[k] = t.x;
+      v[k + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; k++) v[k] = p[k];
+  }
+}
+
+// store w[0..N-2] (the row without its last point)
+template <int N>
+__device__ __forceinline__ void store_row_head(double *p, const double (&w)[N - 1])
+{
+  if constexpr (N % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k + 1 < N - 1; k += 2) *reinterpret_cast<double2 *>(p + k) = make_double2(w[k], w[k + 1]);
+    p[N - 2] = w[N - 2];
+  } else {
+#pragma unroll
+    for (int k = 0; k < N - 1; k++) p[k] = w[k];
+  }
+}
+
+// y then z pairs of C values per slot.  pres: this slot holds an x-level
+// value; ypres: it holds a y-level value; pzpres: its z partner does.
+template <int C>
+__device__ __forceinline__ void yz_pairs(double (&w)[C], bool pres, bool yseam, int ylane, bool ppres_y, bool zseam,
+                                         bool ypres, bool pzpres, double *zbuf_mine, const double *zbuf_peer,
+                                         int bar_id, int bar_n)
+{
+  // y pairs: every lane of the warp takes part in the shuffle
+#pragma unroll
+  for (int k = 0; k < C; k++) {
+    const double o = __shfl_sync(0xffffffffu, w[k], ylane);
+    if (yseam) w[k] = pres ? (ppres_y ? w[k] + o : w[k]) : o;
+  }
+  // z pairs through shared memory
+  if (zseam && ypres) {
+#pragma unroll
+    for (int k = 0; k < C; k++) zbuf_mine[k] = w[k];
+  }
+  asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(bar_n) : "memory");
+  if (zseam) {
+#pragma unroll
+    for (int k = 0; k < C; k++) {
+      const double o = zbuf_peer[k];
+      w[k] = ypres ? (pzpres ? w[k] + o : w[k]) : o;
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) rows_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int P = pow2_at_least(N);
+  constexpr int TT = tile_threads(N);
+  constexpr int NV = N - 1;  // values per slot and element: seam + row[1..N-2]
+  extern __shared__ double zx[];  // [tile][parity][side][P][NV]
+  const int lt = threadIdx.x / TT;
+  const int slot = threadIdx.x % TT;
+  const long tile = (long)blockIdx.x * p.tiles_per_block + lt;
+  if (tile >= p.ntiles) return;  // the whole tile leaves together
+  const TileCoords t = tile_coords(f, p, tile);
+  if (t.skip) return;
+  const int sy = slot % P, sz = slot / P;
+  SlotSetup s;
+  slot_setup(f, t, sy, sz, P, s);
+
+  const bool ypres = s.valid || s.pvy;
+  const bool pzpres = s.pvz || s.pvyz;
+  const int lane = threadIdx.x & 31;
+  const int syp = (sy == 0) ? N - 1 : 0;
+  const int ylane = s.yseam ? (lane - sy + syp) : lane;
+  double *zt = zx + (long)lt * 2 * 2 * P * NV;
+  const int side = (sz == 0) ? 0 : 1;
+  const int bar_id = 1 + lt;
+  const bool interior_row = !(s.yseam || s.zseam);
+  const double *rd = s.rd;
+  const long es = s.es;
+
+  // the previous element's last point: the x-lower copy of the first seam
+  double carry = 0.0;
+  bool hc = false;
+  double *carry_w = nullptr;
+  if (s.lo) {
+    carry = *s.lo;
+    hc = true;
+    carry_w = s.lo_w ? const_cast<double *>(s.lo) : nullptr;
+  }
+
+  double cur[N], nxt[N];
+  if (s.valid) load_row<N>(cur, rd + (long)t.jx0 * es);
+  int par = 0;
+  for (int jx = t.jx0; jx < t.jx1; jx++) {
+    if (s.valid && jx + 1 < t.jx1) load_row<N>(nxt, rd + (long)(jx + 1) * es);
+    double w[NV];
+    w[0] = hc ? carry + cur[0] : cur[0];
+#pragma unroll
+    for (int k = 1; k < NV; k++) w[k] = cur[k];
+    yz_pairs<NV>(w, s.valid, s.yseam, ylane, s.pvy, s.zseam, ypres, pzpres,
+                 zt + ((par * 2 + side) * P + sy) * NV, zt + ((par * 2 + (1 - side)) * P + sy) * NV, bar_id, TT);
+    par ^= 1;
+    if (s.writable) {
+      double *row = const_cast<double *>(rd) + (long)jx * es;
+      if (interior_row) row[0] = w[0];
+      else store_row_head<N>(row, w);
+    }
+    if (carry_w) *carry_w = w[0];
+    if (s.valid) {
+      carry = cur[N - 1];
+      hc = true;
+      carry_w = s.writable ? const_cast<double *>(rd) + (long)jx * es + (N - 1) : nullptr;
+    }
+#pragma unroll
+    for (int k = 0; k < N; k++) cur[k] = nxt[k];
+  }
+
+  if (t.hi_x) {
+    // the seam between element mx-1 and the x-upper neighbour (or nothing)
+    double w[1];
+    w[0] = s.hi ? carry + *s.hi : carry;
+    yz_pairs<1>(w, s.valid, s.yseam, ylane, s.pvy, s.zseam, ypres, pzpres,
+                zt + ((par * 2 + side) * P + sy) * NV, zt + ((par * 2 + (1 - side)) * P + sy) * NV, bar_id, TT);
+    if (carry_w) *carry_w = w[0];
+  }
+}
+
+bool row_kernel_supported(int n) { return n >= 2 && n <= 16; }
+
+template <int N>
+static cudaError_t launch_rows_n(const FieldDesc &f, const RowPlan &p, cudaStream_t s)
+{
+  constexpr int P = pow2_at_least(N);
+  const int threads = p.tiles_per_block * tile_threads(N);
+  const size_t smem = sizeof(double) * p.tiles_per_block * 2 * 2 * P * (N - 1);
+  const long blocks = (p.ntiles + p.tiles_per_block - 1) / p.tiles_per_block;
+  if (blocks == 0) return cudaSuccess;
+  rows_kernel<N><<<(unsigned)blocks, threads, smem, s>>>(f, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s)
+{
+  switch (f.n) {
+    case 2: return launch_rows_n<2>(f, p, s);
+    case 3: return launch_rows_n<3>(f, p, s);
+    case 4: return launch_rows_n<4>(f, p, s);
+    case 5: return launch_rows_n<5>(f, p, s);
+    case 6: return launch_rows_n<6>(f, p, s);
+    case 7: return launch_rows_n<7>(f, p, s);
+    case 8: return launch_rows_n<8>(f, p, s);
+    case 9: return launch_rows_n<9>(f, p, s);
+    case 10: return launch_rows_n<10>(f, p, s);
+    case 11: return launch_rows_n<11>(f, p, s);
+    case 12: return launch_rows_n<12>(f, p, s);
+    case 13: return launch_rows_n<13>(f, p, s);
+    case 14: return launch_rows_n<14>(f, p, s);
+    case 15: return launch_rows_n<15>(f, p, s);
+    case 16: return launch_rows_n<16>(f, p, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// check: closed form of s shares from a known initial state
+// ---------------------------------------------------------------------------
+//
+// After one share every copy of a point holds S, the tree sum of its initial
+// copies; a later share sums c equal copies (c = 2^k, k = number of seam
+// axes), which the tree does exactly: c*S.  So after s shares every copy
+// holds S * 2^(k*(s-1)).  With compute = false only points on the subdomain
+// boundary are summed (gpu/main.cc:157-161, gpu/Mugs.cc:146-150).
+
+__device__ __forceinline__ double init_at(const FieldDesc &f, int init, uint64_t seed, int q, int ix, int iy, int iz,
+                                          int jx, int jy, int jz)
+{
+  if (init == 0) return ref_value(ix, iy, iz, jx, jy, jz);
+  return int_value(seed, (long)q * f.R + elem_index(f, ix, iy, iz, jx, jy, jz));
+}
+
+__global__ void check_kernel(FieldDesc f, int init, unsigned long long seed, int nshares, int compute,
+                             unsigned long long *rank_max, unsigned long long *gmax, unsigned long long target,
+                             unsigned long long *first, long only, double *vals)
+{
+  const int n = f.n;
+  const long per_elem = (long)n * n * n;
+  const long per_rank = per_elem * f.m[0] * f.m[1] * f.m[2];
+  const long total = only >= 0 ? only + 1 : per_rank * f.nranks;
+  const long p0 = only >= 0 ? only : 0;
+  for (long p = p0 + blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(p / per_rank);
+    long t = p % per_rank;
+    int i[3], j[3];
+    i[0] = (int)(t % n); t /= n;
+    i[1] = (int)(t % n); t /= n;
+    i[2] = (int)(t % n); t /= n;
+    j[0] = (int)(t % f.m[0]); t /= f.m[0];
+    j[1] = (int)(t % f.m[1]); t /= f.m[1];
+    j[2] = (int)t;
+    // copies along each axis: (rank offset, element, point) for lower/upper
+    int cnt[3], dd[3][2], ee[3][2], ii[3][2];
+    bool onb = false;
+    int k = 0;
+    for (int a = 0; a < 3; a++) {
+      const int m = f.m[a];
+      const int g = j[a] * (n - 1) + i[a];
+      onb |= (g == 0 || g == m * (n - 1));
+      cnt[a] = 1;
+      dd[a][0] = 0; ee[a][0] = j[a]; ii[a][0] = i[a];
+      int dv[3] = {0, 0, 0};
+      if (i[a] == 0) {
+        // seam with the element below: lower copy (j-1, n-1), upper copy self
+        bool has = j[a] > 0;
+        int dlo = 0, elo = j[a] - 1;
+        if (!has) {
+          dv[a] = -1;
+          has = nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) >= 0;
+          dlo = -1; elo = m - 1;
+        }
+        if (has) {
+          cnt[a] = 2;
+          dd[a][0] = dlo; ee[a][0] = elo; ii[a][0] = n - 1;
+          dd[a][1] = 0; ee[a][1] = j[a]; ii[a][1] = 0;
+        }
+      } else if (i[a] == n - 1) {
+        // seam with the element above: lower copy self, upper copy (j+1, 0)
+        bool has = j[a] < m - 1;
+        int dhi = 0, ehi = j[a] + 1;
+        if (!has) {
+          dv[a] = 1;
+          has = nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) >= 0;
+          dhi = 1; ehi = 0;
+        }
+        if (has) {
+          cnt[a] = 2;
+          dd[a][1] = dhi; ee[a][1] = ehi; ii[a][1] = 0;
+        }
+      }
+      if (cnt[a] == 2) k++;
+    }
+    double expect;
+    const double self = init_at(f, init, seed, r, i[0], i[1], i[2], j[0], j[1], j[2]);
+    if (nshares == 0 || k == 0 || (!compute && !onb)) {
+      expect = self;
+    } else {
+      double sy[2];
+      for (int bz = 0; bz < cnt[2]; bz++) {
+        double sx[2];
+        for (int by = 0; by < cnt[1]; by++) {
+          for (int bx = 0; bx < cnt[0]; bx++) {
+            const int dx = dd[0][bx], dyy = dd[1][by], dzz = dd[2][bz];
+            const int q = (dx | dyy | dzz) ? nbr_of(f, r, dir_index(dx, dyy, dzz)) : r;
+            const double v = init_at(f, init, seed, q, ii[0][bx], ii[1][by], ii[2][bz], ee[0][bx], ee[1][by], ee[2][bz]);
+            sx[by] = bx ? sx[by] + v : v;
+          }
+        }
+        sy[bz] = (cnt[1] == 2) ? sx[0] + sx[1] : sx[0];
+      }
+      const double S = (cnt[2] == 2) ? sy[0] + sy[1] : sy[0];
+      expect = scalbn(S, k * (nshares - 1));
+    }
+    const double got = f.u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+    const double denom = fabs(got) + fabs(expect);
+    double d = (denom > 1e-15) ? fabs(got - expect) / denom : 0.0;
+    if (d != d) d = __longlong_as_double(0x7ff0000000000000LL);  // NaN counts as infinite error
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+    if (only >= 0) {
+      vals[0] = got;
+      vals[1] = expect;
+    } else if (target) {
+      if (bits == target) atomicMin(first, (unsigned long long)p);
+    } else if (bits) {
+      atomicMax(rank_max + r, bits);
+      atomicMax(gmax, bits);
+    }
+  }
+}
+
+cudaError_t launch_check(const FieldDesc &f, int init, unsigned long long seed, int nshares, int compute,
+                         unsigned long long *rank_max, unsigned long long *gmax, unsigned long long target,
+                         unsigned long long *first, long only, double *vals, cudaStream_t s)
+{
+  if (only >= 0) check_kernel<<<1, 1, 0, s>>>(f, init, seed, nshares, compute, rank_max, gmax, target, first, only, vals);
+  else check_kernel<<<152 * 8, 256, 0, s>>>(f, init, seed, nshares, compute, rank_max, gmax, target, first, -1, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_ref(const FieldDesc &f, cudaStream_t s)
+{
+  init_ref_kernel<<<152 * 8, 256, 0, s>>>(f, f.R * f.nranks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStream_t s)
+{
+  init_int_kernel<<<152 * 8, 256, 0, s>>>(f, f.R * f.nranks, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
+{
+  long maxsz = 0;
+  const int dface[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int a = 0; a < 3; a++) {
+    const long sz = region_size(f, dface[a]);
+    if (sz > maxsz) maxsz = sz;
+  }
+  long bx = (maxsz + 255) / 256;
+  if (bx > 4096) bx = 4096;
+  if (bx < 1) bx = 1;
+  dim3 grid((unsigned)bx, (unsigned)(f.nranks * 27));
+  pack_kernel<<<grid, 256, 0, s>>>(f);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s)
+{
+  gather_kernel<<<152 * 16, 256, 0, s>>>(f, compute);
+  return cudaGetLastError();
+}
+
+}  // namespace faces

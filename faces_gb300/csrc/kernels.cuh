@@ -1,0 +1,31 @@
+// kernels.cuh -- launch wrappers for the sm_103a halo-sum kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "geom.cuh"
+#include "rows_setup.cuh"
+
+namespace faces {
+
+bool row_kernel_supported(int n);
+
+cudaError_t launch_init_ref(const FieldDesc &f, cudaStream_t s);
+cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStream_t s);
+cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s);
+cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s);
+cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
+
+// Closed-form check of a field after `nshares` shares of a known initial
+// state (init: 0 = reference formula, 1 = integer seed) with the relative
+// error rule of gpu/main.cc:39-105.  Pass 1 (target = 0) raises rank_max[r]
+// (per-rank maximum error as an ordered 64-bit pattern; zeroed by the
+// caller) and *gmax.  Pass 2 (target = the maximum's pattern) lowers *first
+// (set to ~0 by the caller) to the first linear point index with that error.
+// Pass 3 (only >= 0) writes (u, expected) of point `only` into vals[2].
+// Linear point index = ((((r*mz + jz)*my + jy)*mx + jx)*n + iz)*n*n + iy*n + ix.
+cudaError_t launch_check(const FieldDesc &f, int init, unsigned long long seed, int nshares, int compute,
+                         unsigned long long *rank_max, unsigned long long *gmax, unsigned long long target,
+                         unsigned long long *first, long only, double *vals, cudaStream_t s);
+
+}  // namespace faces

@@ -1,0 +1,121 @@
+/*
+ * faces_gb300.h -- C ABI of the GB300 (sm_103a) Faces halo-sum library.
+ *
+ * One context replaces the reference's per-rank `Faces` object
+ * (gpu/v-26-messages/Faces.h:6-39) for all lx*ly*lz ranks at once: the MPI
+ * rank grid becomes lx*ly*lz virtual ranks held in one device allocation,
+ * rank-major.  Each rank's part uses the reference's DArray<double,6> layout
+ * (gpu/DArray.h:34-38,91-101):
+ *     idx = ix + n*iy + n^2*iz + n^3*jx + n^3*mx*jy + S4*jz,
+ *     S4  = ceil(n^3*mx*my/512)*512,     rank stride = S4*mz.
+ *
+ * One share makes every point shared by 2 (face), 4 (edge) or 8 (corner)
+ * element copies -- inside a rank and across its 26 neighbour ranks -- equal
+ * to the FP64 sum of its copies.  The sum is formed as a tree in dimension
+ * order (x pairs, then y pairs, then z pairs), the order of the reference's
+ * Mugs oracle (gpu/Mugs.cc:140-202).
+ *
+ * Conventions: every call returns FACES_OK (0) or a negative FACES_E* code
+ * and records a message for faces_last_error(); no exception crosses the ABI.
+ * Device pointers must be 16-byte aligned (cudaMalloc gives 256).  `stream`
+ * is a cudaStream_t (NULL: the legacy default stream).  Calls that take a
+ * stream only enqueue work on it unless stated otherwise.  A context may be
+ * used by one host thread at a time.
+ */
+#ifndef FACES_GB300_H
+#define FACES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FACES_OK 0
+#define FACES_EINVAL (-1)       /* bad argument */
+#define FACES_ECUDA (-2)        /* a CUDA call failed */
+#define FACES_ENOMEM (-3)       /* device or host allocation failed */
+#define FACES_EALIGN (-4)       /* pointer not 16-byte aligned */
+#define FACES_EUNSUPPORTED (-5) /* combination not implemented */
+
+/* faces_create flags */
+#define FACES_PERIODIC 0x1u /* neighbours wrap around the rank grid; the
+                               reference has none (MPI_PROC_NULL outside,
+                               gpu/v-26-messages/Faces.cc:92-103) */
+#define FACES_MESSAGES 0x2u /* v-26 strategy: every rank packs its 26 boundary
+                               messages, the buffers are swapped by direction,
+                               each rank unpack-adds its own copies.  Without
+                               it one owner sums each shared point across
+                               ranks in place (same values, no messages). */
+#define FACES_GATHER 0x4u   /* force the generic one-thread-per-point kernel */
+
+typedef struct faces_ctx faces_ctx;
+
+/* Faces::Faces(rank,lx,ly,lz,mx,my,mz,n) for every rank at once
+ * (gpu/v-26-messages/Faces.cc:10-82): neighbour tables, message buffers. */
+int faces_create(faces_ctx **ctx, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags);
+
+/* Faces::~Faces (gpu/v-26-messages/Faces.cc:84-90).  NULL is accepted. */
+int faces_destroy(faces_ctx *ctx);
+
+/* DArray<double,6> strides of one rank (gpu/DArray.h:34-38; stride of ix is
+ * 1, strides[0..5] are those of ix, iy, iz, jx, jy, jz), the doubles per rank
+ * and in the whole field.  Any pointer may be NULL. */
+int faces_layout(const faces_ctx *ctx, long strides[6], long *rank_doubles, long *total_doubles);
+
+/* DArray's allocation (gpu/DArray.h:77-82): a zero-filled device field for
+ * all ranks.  Free with faces_field_free. */
+int faces_field_alloc(const faces_ctx *ctx, double **u);
+int faces_field_free(double *u);
+
+/* Faces::share(u, compute) (gpu/v-26-messages/Faces.h:18,
+ * gpu/v-26-messages/Faces.cc:111-678) on every rank.  compute = 0 is the
+ * reference's "shares without compute kernels" (gpu/main.cc:157-161): only
+ * points on a subdomain boundary are summed.  Stream-ordered: returns once
+ * the work is enqueued (the reference's share returns after completion;
+ * synchronize the stream for that). */
+int faces_share(faces_ctx *ctx, double *u, int compute, void *stream);
+
+/* nshares consecutive shares (the `ni` loop of gpu/main.cc:180). */
+int faces_share_n(faces_ctx *ctx, double *u, int compute, int nshares, void *stream);
+
+/* gpu/main.cc:10-19: u(ix,iy,iz,jx,jy,jz) = jz*1e4 + jy*100 + jx + iz*0.01 +
+ * iy*1e-4 + ix*1e-6 on every rank, each product and sum rounded once;
+ * padding zero. */
+int faces_init_ref(faces_ctx *ctx, double *u, void *stream);
+
+/* integer-valued doubles uniform in [0,2^20): the top 20 bits of
+ * splitmix64(seed*0x9E3779B97F4A7C15 + linear index); padding zero. */
+int faces_init_int(faces_ctx *ctx, double *u, unsigned long long seed, void *stream);
+
+/* The correctness check of gpu/main.cc:39-105 without a host copy: compares
+ * u, after `nshares` shares (compute as given) of the initial state `init`
+ * (0: faces_init_ref, 1: faces_init_int with `seed`), with the closed form
+ * (every copy of a point with k seam axes holds S*2^(k*(s-1)), S the tree
+ * sum of its initial copies).  Outputs (each may be NULL): rank_maxrel[nranks]
+ * the per-rank maximum relative error |u-v|/(|u|+|v|); *npass the ranks
+ * below 1e-15; where[7] = rank, ix, iy, iz, jx, jy, jz of the largest error
+ * and vals[2] = (u, expected) there.  Synchronous. */
+int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long seed, int nshares, int compute,
+                double *rank_maxrel, double *maxrel, int *npass, int where[7], double vals[2], void *stream);
+
+/* End-to-end call for host data: copies u_in (host, total doubles) to the
+ * context's device field, runs nshares shares, copies the result to u_out
+ * (host; may equal u_in).  Synchronous.  Pinned host memory is fastest. */
+int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int compute, int nshares, void *stream);
+
+/* Work decomposition of the row kernel: elements per x-chunk (<= 0: default)
+ * and tiles per thread block (<= 0: default). */
+int faces_set_tuning(faces_ctx *ctx, int chunk, int tiles_per_block);
+
+/* Kernel launches one share enqueues with the current settings. */
+int faces_launches_per_share(const faces_ctx *ctx, int compute);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *faces_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FACES_GB300_H */

@@ -1,0 +1,212 @@
+// rows_emu.cc -- CPU replay of the row kernel (test infrastructure).
+//
+// Runs the kernel's own tile/slot setup (faces_gb300/csrc/rows_setup.cuh) for
+// every tile and slot of a share and emulates one thread block in lockstep:
+// x pairs per slot, then y pairs, then z pairs, then the stores.  Checks that
+// every pointer stays inside the field or the message buffers and that no
+// field point is written more than once per share.  The message mode's pack
+// is replayed from region(d) as the pack kernel does.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "geom.cuh"
+#include "rows_setup.cuh"
+#include "tables.h"
+
+using namespace faces;
+
+namespace {
+
+struct Ctx {
+  FieldDesc f;
+  const double *u0, *u1, *m0, *m1;
+  std::vector<unsigned char> wcount;
+  std::string err;
+  bool ok = true;
+};
+
+bool in_field(const Ctx &c, const double *p, long len)
+{
+  return p >= c.u0 && p + len <= c.u1;
+}
+
+bool in_any(const Ctx &c, const double *p, long len)
+{
+  return in_field(c, p, len) || (c.m0 && p >= c.m0 && p + len <= c.m1);
+}
+
+void bad(Ctx &c, const char *what, long tile, int sy, int sz, int jx)
+{
+  if (!c.ok) return;
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s (tile %ld slot %d,%d jx %d)", what, tile, sy, sz, jx);
+  c.err = buf;
+  c.ok = false;
+}
+
+void write(Ctx &c, double *p, double v, long tile, int sy, int sz, int jx)
+{
+  if (!in_field(c, p, 1)) { bad(c, "write outside the field", tile, sy, sz, jx); return; }
+  const long k = p - c.u0;
+  if (c.wcount[k]++) { bad(c, "point written twice", tile, sy, sz, jx); return; }
+  *p = v;
+}
+
+void pack(FieldDesc &f)
+{
+  const int n = f.n;
+  for (int r = 0; r < f.nranks; r++)
+    for (int dir = 0; dir < 27; dir++) {
+      if (dir == 13 || f.msg_off[r * 27 + dir] < 0) continue;
+      const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
+      const long sz = region_size(f, d);
+      for (long pos = 0; pos < sz; pos++) {
+        int i[3], j[3];
+        long t = pos;
+        for (int a = 0; a < 3; a++)
+          if (d[a] == 0) { i[a] = (int)(t % n); t /= n; }
+        for (int a = 0; a < 3; a++)
+          if (d[a] == 0) { j[a] = (int)(t % f.m[a]); t /= f.m[a]; }
+        for (int a = 0; a < 3; a++)
+          if (d[a] != 0) { i[a] = d[a] < 0 ? 0 : n - 1; j[a] = d[a] < 0 ? 0 : f.m[a] - 1; }
+        f.msg[f.msg_off[r * 27 + dir] + pos] = f.u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+      }
+    }
+}
+
+// one tile, all slots in lockstep
+void run_tile(Ctx &c, const RowPlan &p, long tile)
+{
+  const FieldDesc &f = c.f;
+  const int n = f.n, P = pow2_at_least(n), NV = n - 1;
+  const TileCoords t = tile_coords(f, p, tile);
+  if (t.skip) return;
+  const int S = P * n;
+  std::vector<SlotSetup> ss(S);
+  for (int sl = 0; sl < S; sl++) slot_setup(f, t, sl % P, sl / P, P, ss[sl]);
+  std::vector<double> carry(S, 0.0), cur(S * n), w(S * NV), wy(S * NV);
+  std::vector<char> hc(S, 0);
+  std::vector<double *> carry_w(S, nullptr);
+  for (int sl = 0; sl < S; sl++) {
+    const SlotSetup &s = ss[sl];
+    if (s.lo) {
+      if (!in_any(c, s.lo, 1)) bad(c, "lo end outside buffers", tile, sl % P, sl / P, -1);
+      if (s.lo_w && !in_field(c, s.lo, 1)) bad(c, "writable lo end outside field", tile, sl % P, sl / P, -1);
+      if (!c.ok) return;
+      carry[sl] = *s.lo;
+      hc[sl] = 1;
+      carry_w[sl] = s.lo_w ? const_cast<double *>(s.lo) : nullptr;
+    }
+  }
+  auto pairs = [&](int C) {
+    // y pairs
+    for (int sl = 0; sl < S; sl++) {
+      const SlotSetup &s = ss[sl];
+      const int sy = sl % P, sz = sl / P;
+      for (int k = 0; k < C; k++) wy[sl * NV + k] = w[sl * NV + k];
+      if (!s.yseam) continue;
+      const int syp = sy == 0 ? n - 1 : 0;
+      const int pl = syp + P * sz;
+      for (int k = 0; k < C; k++) {
+        const double o = w[pl * NV + k];
+        wy[sl * NV + k] = s.valid ? (s.pvy ? w[sl * NV + k] + o : w[sl * NV + k]) : o;
+      }
+    }
+    // z pairs
+    for (int sl = 0; sl < S; sl++) {
+      const SlotSetup &s = ss[sl];
+      const int sy = sl % P, sz = sl / P;
+      for (int k = 0; k < C; k++) w[sl * NV + k] = wy[sl * NV + k];
+      if (!s.zseam) continue;
+      const int szp = sz == 0 ? n - 1 : 0;
+      const int pl = sy + P * szp;
+      const bool ypres = s.valid || s.pvy, pzpres = s.pvz || s.pvyz;
+      for (int k = 0; k < C; k++) {
+        const double o = wy[pl * NV + k];
+        w[sl * NV + k] = ypres ? (pzpres ? wy[sl * NV + k] + o : wy[sl * NV + k]) : o;
+      }
+    }
+  };
+  for (int jx = t.jx0; jx < t.jx1; jx++) {
+    for (int sl = 0; sl < S; sl++) {
+      const SlotSetup &s = ss[sl];
+      if (!s.valid) continue;
+      const double *row = s.rd + (long)jx * s.es;
+      if (!in_any(c, row, n)) { bad(c, "row read outside buffers", tile, sl % P, sl / P, jx); return; }
+      for (int k = 0; k < n; k++) cur[sl * n + k] = row[k];
+      w[sl * NV] = hc[sl] ? carry[sl] + cur[sl * n] : cur[sl * n];
+      for (int k = 1; k < NV; k++) w[sl * NV + k] = cur[sl * n + k];
+    }
+    pairs(NV);
+    for (int sl = 0; sl < S; sl++) {
+      const SlotSetup &s = ss[sl];
+      if (s.writable) {
+        double *row = const_cast<double *>(s.rd) + (long)jx * s.es;
+        const bool interior = !(s.yseam || s.zseam);
+        if (interior) write(c, row, w[sl * NV], tile, sl % P, sl / P, jx);
+        else for (int k = 0; k < NV; k++) write(c, row + k, w[sl * NV + k], tile, sl % P, sl / P, jx);
+      }
+      if (carry_w[sl]) write(c, carry_w[sl], w[sl * NV], tile, sl % P, sl / P, jx);
+      if (!c.ok) return;
+      if (s.valid) {
+        carry[sl] = cur[sl * n + n - 1];
+        hc[sl] = 1;
+        carry_w[sl] = s.writable ? const_cast<double *>(s.rd) + (long)jx * s.es + n - 1 : nullptr;
+      }
+    }
+  }
+  if (t.hi_x) {
+    for (int sl = 0; sl < S; sl++) {
+      const SlotSetup &s = ss[sl];
+      if (s.hi && !in_any(c, s.hi, 1)) { bad(c, "hi end outside buffers", tile, sl % P, sl / P, f.m[0]); return; }
+      w[sl * NV] = s.hi ? carry[sl] + *s.hi : carry[sl];
+    }
+    pairs(1);
+    for (int sl = 0; sl < S; sl++)
+      if (carry_w[sl]) write(c, carry_w[sl], w[sl * NV], tile, sl % P, sl / P, f.m[0]);
+  }
+}
+
+}  // namespace
+
+extern "C" int rows_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int messages,
+                            int chunk, int tiles_per_block, double *u, int nsteps, char *err, int errlen)
+{
+  Ctx c;
+  FieldDesc &f = c.f;
+  f.n = n;
+  f.m[0] = mx; f.m[1] = my; f.m[2] = mz;
+  f.L[0] = lx; f.L[1] = ly; f.L[2] = lz;
+  f.periodic = periodic;
+  f.mode = messages ? kMessages : kDirect;
+  f.nranks = lx * ly * lz;
+  f.sjy = (long)n * n * n * mx;
+  f.sjz = jz_stride(n, mx, my);
+  f.R = f.sjz * mz;
+  f.u = u;
+  std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
+  std::vector<long> off;
+  long mtot = messages ? message_offsets(f, nbr, off) : 0;
+  if (!messages) off.assign(nbr.size(), -1);
+  std::vector<double> msg(mtot > 0 ? mtot : 1, 0.0);
+  f.nbr = nbr.data();
+  f.msg_off = off.data();
+  f.msg = messages ? msg.data() : nullptr;
+  c.u0 = u;
+  c.u1 = u + f.R * f.nranks;
+  c.m0 = messages ? msg.data() : nullptr;
+  c.m1 = messages ? msg.data() + mtot : nullptr;
+  const RowPlan p = make_row_plan(f, chunk > 0 ? chunk : mx, tiles_per_block);
+  for (int step = 0; step < nsteps && c.ok; step++) {
+    c.wcount.assign(f.R * f.nranks, 0);
+    if (messages) pack(f);
+    for (long tile = 0; tile < p.ntiles && c.ok; tile++) run_tile(c, p, tile);
+  }
+  if (!c.ok) {
+    snprintf(err, errlen, "%s", c.err.c_str());
+    return -1;
+  }
+  return 0;
+}

@@ -1,0 +1,110 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle, bit for bit.
+
+Every kernel forms each shared point's sum as the tree x pairs -> y pairs ->
+z pairs, the order of the reference's Mugs passes (gpu/Mugs.cc:140-202), so
+the comparison is exact for any input -- integer-valued (where every order is
+exact) and the reference's non-integer init (gpu/main.cc:18) alike.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+
+def run_gpu(F, s, *, periodic, messages, gather=False, init="int", seed=5, nsteps=2, compute=True):
+    f = F.Faces(s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n, periodic=periodic, messages=messages, gather=gather)
+    u = f.field()
+    if init == "int":
+        f.init_int(u, seed)
+    else:
+        f.init_ref(u)
+    u_init = u.cpu().numpy()
+    f.share_n(u, nsteps, compute)
+    torch.cuda.synchronize()
+    out = u.cpu().numpy()
+    chk = f.check(u, init=init, seed=seed, nshares=nsteps, compute=compute)
+    f.close()
+    return u_init, out, chk
+
+
+SHAPES = [
+    # lx ly lz mx my mz n
+    (1, 1, 1, 4, 4, 4, 5),      # the C1 shape
+    (1, 1, 1, 3, 2, 5, 8),
+    (1, 1, 1, 1, 1, 1, 3),
+    (1, 1, 1, 2, 3, 1, 2),
+    (2, 1, 1, 3, 2, 2, 4),
+    (1, 2, 2, 2, 3, 2, 6),
+    (3, 3, 3, 2, 2, 2, 6),      # the C3 rank grid, small elements
+    (2, 2, 2, 1, 1, 1, 7),
+    (1, 1, 1, 5, 2, 3, 10),
+    (2, 1, 2, 2, 2, 1, 12),
+    (1, 1, 1, 2, 2, 2, 16),
+    (1, 3, 1, 3, 1, 2, 9),
+]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+@pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
+def test_rows_bit_exact(oracle, faces_lib, shape, periodic, messages):
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=periodic)
+    for init in ("int", "ref"):
+        u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, init=init, nsteps=3)
+        ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
+        assert np.array_equal(u_init, ref0), "device init differs from the host formula"
+        exp = O.groups_share(s, ref0.copy(), True, 3)
+        assert np.array_equal(out, exp), f"{init}: {np.count_nonzero(out != exp)} points differ"
+        assert chk.passed and chk.npass == s.nranks
+
+
+@pytest.mark.parametrize("shape", SHAPES[:8], ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+@pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
+def test_without_compute_kernels(oracle, faces_lib, shape, periodic, messages):
+    """ni < 0 in the reference: only points on a subdomain boundary are summed."""
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=periodic)
+    u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, compute=False, nsteps=2)
+    exp = O.groups_share(s, O.init_int(s, 5), False, 2)
+    assert np.array_equal(out, exp)
+    assert chk.passed
+
+
+@pytest.mark.parametrize("shape", SHAPES[:6], ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
+def test_gather_kernel(oracle, faces_lib, shape, messages):
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=True)
+    _, out, _ = run_gpu(F, s, periodic=True, messages=messages, gather=True, init="ref", nsteps=2)
+    assert np.array_equal(out, O.groups_share(s, O.init_ref(s), True, 2))
+
+
+def test_mugs_bit_exact_single_rank(oracle, faces_lib):
+    """One non-periodic rank: equal to the Mugs restatement (and so to the
+    reference's own Mugs) bit for bit on the reference init."""
+    O, F = oracle, faces_lib
+    s = O.Shape(1, 1, 1, 3, 4, 2, 6)
+    _, out, _ = run_gpu(F, s, periodic=False, messages=False, init="ref", nsteps=4)
+    assert np.array_equal(out, O.mugs_share(s, O.init_ref(s), True, 4))
+
+
+@pytest.mark.parametrize("chunk", [1, 2, 3, 5])
+def test_chunking(oracle, faces_lib, chunk):
+    O, F = oracle, faces_lib
+    for periodic, messages in itertools.product([False, True], [False, True]):
+        s = O.Shape(2, 1, 1, 7, 2, 2, 5, periodic=periodic)
+        f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages)
+        f.set_tuning(chunk=chunk, tiles_per_block=1 + chunk % 3)
+        u = f.field()
+        f.init_ref(u)
+        f.share_n(u, 2)
+        torch.cuda.synchronize()
+        assert np.array_equal(u.cpu().numpy(), O.groups_share(s, O.init_ref(s), True, 2))
