@@ -16,7 +16,7 @@ import ctypes
 import os
 from dataclasses import dataclass
 
-__all__ = ["Faces", "FacesError", "lib", "library_path", "PERIODIC", "MESSAGES", "GATHER"]
+__all__ = ["Faces", "FacesError", "lib", "library_path", "PERIODIC", "MESSAGES", "GATHER", "ROWS"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 library_path = os.path.join(HERE, "lib", "libfaces_gb300.so")
@@ -25,6 +25,7 @@ exe_path = os.path.join(HERE, "bin", "faces")
 PERIODIC = 0x1
 MESSAGES = 0x2
 GATHER = 0x4
+ROWS = 0x8
 
 _ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
 
@@ -63,7 +64,7 @@ def lib() -> ctypes.CDLL:
                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                               ctypes.POINTER(ctypes.c_double), vp]
     L.faces_run_host.argtypes = [vp, dp, dp, c_int, c_int, vp]
-    L.faces_set_tuning.argtypes = [vp, c_int, c_int]
+    L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
     L.faces_last_error.restype = ctypes.c_char_p
     for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
@@ -126,16 +127,18 @@ class Faces:
     messages -- v-26 strategy: 26 messages per rank packed, swapped by buffer
                 direction and unpack-added (else one owner per shared point)
     gather   -- force the generic one-thread-per-point kernel
+    rows     -- use the register row kernel instead of the shared-memory tiles
     """
 
     def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
-                 periodic: bool = False, messages: bool = False, gather: bool = False):
-        flags = (PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
+                 periodic: bool = False, messages: bool = False, gather: bool = False, rows: bool = False):
+        flags = ((PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
+                 | (ROWS if rows else 0))
         h = ctypes.c_void_p()
         _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
         self._h = h
         self.shape = (lx, ly, lz, mx, my, mz, n)
-        self.periodic, self.messages, self.gather = periodic, messages, gather
+        self.periodic, self.messages, self.gather, self.rows = periodic, messages, gather, rows
         s = (ctypes.c_long * 6)()
         rd, tot = ctypes.c_long(), ctypes.c_long()
         _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
@@ -217,8 +220,11 @@ class Faces:
         _check(lib().faces_run_host(self._h, u_in.ctypes.data, u_out.ctypes.data, int(compute), nshares,
                                     _stream(stream)))
 
-    def set_tuning(self, chunk: int = 0, tiles_per_block: int = 0) -> None:
-        _check(lib().faces_set_tuning(self._h, chunk, tiles_per_block))
+    def set_tuning(self, chunk: int = 0, width: int = 0, order: int = -1) -> None:
+        """Elements per x-chunk, width (row kernel: tiles per block; tile
+        kernel: resident blocks per SM) and tile order (0 strided, 1
+        contiguous); 0 / -1 keep the defaults."""
+        _check(lib().faces_set_tuning(self._h, chunk, width, order))
 
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))

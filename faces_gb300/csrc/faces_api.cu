@@ -65,8 +65,11 @@ struct faces_ctx {
   double *d_msg = nullptr;
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
   double *d_field = nullptr;                // faces_run_host's device copy
-  int chunk = 0, tpb = 0;
-  RowPlan plan;
+  int chunk = 0, tpb = 0, order = -1;
+  int sms = 0;       // multiprocessors of the device
+  RowPlan plan;      // row kernel
+  RowPlan tplan;     // tile kernel
+  long tgrid = 0;    // tile kernel CTAs
 
   FieldDesc desc(double *u) const
   {
@@ -106,6 +109,20 @@ void replan(faces_ctx &c)
 {
   const FieldDesc f = c.desc(nullptr);
   c.plan = make_row_plan(f, c.chunk > 0 ? c.chunk : default_chunk(c), c.tpb);
+  if (tile_kernel_supported(c.n)) {
+    // the tile kernel is built for 1, 2, 4 or 8 elements per tile
+    int k = c.chunk > 0 ? c.chunk : tile_default_chunk(c.n);
+    k = k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1;
+    while (k > 1 && tile_smem_bytes(c.n, k) > 110 * 1024) k /= 2;
+    c.tplan = make_row_plan(f, k, 0);
+    c.tplan.order = c.order >= 0 ? c.order : 0;
+    // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved
+    // per block) and 2048 threads of 256-thread blocks
+    int fit = (int)((228 * 1024) / (tile_smem_bytes(c.n, k) + 1024));
+    if (fit > 8) fit = 8;
+    const int per_sm = c.tpb > 0 ? (c.tpb < fit ? c.tpb : fit) : fit;
+    c.tgrid = (long)c.sms * (per_sm < 1 ? 1 : per_sm);
+  }
 }
 
 int check_ctx(const faces_ctx *c)
@@ -134,7 +151,8 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   if (lx < 1 || ly < 1 || lz < 1) return fail(FACES_EINVAL, "rank grid %d x %d x %d must be positive", lx, ly, lz);
   if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
   if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
-  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER)) return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
+  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS))
+    return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
   const long nranks = (long)lx * ly * lz;
   if (nranks > 65535 / 27) return fail(FACES_EINVAL, "%ld ranks: at most %d virtual ranks", nranks, 65535 / 27);
   faces_ctx *c = new (std::nothrow) faces_ctx();
@@ -164,6 +182,12 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
       (c->d_msg && (e = cudaMemset(c->d_msg, 0, sizeof(double) * c->msg_total)) != cudaSuccess)) {
     faces_destroy(c);
     return cuda_fail(e, "faces_create: upload");
+  }
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+    faces_destroy(c);
+    return cuda_fail(e, "faces_create: device query");
   }
   replan(*c);
   *out = c;
@@ -215,11 +239,13 @@ int faces_field_free(double *u)
   return FACES_OK;
 }
 
-int faces_set_tuning(faces_ctx *c, int chunk, int tiles_per_block)
+int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
 {
   if (int rc = check_ctx(c)) return rc;
+  if (order > 1) return fail(FACES_EINVAL, "order = %d: -1 (default), 0 or 1", order);
   c->chunk = chunk > 0 ? chunk : 0;
-  c->tpb = tiles_per_block > 0 ? tiles_per_block : 0;
+  c->tpb = width > 0 ? width : 0;
+  c->order = order;
   replan(*c);
   return FACES_OK;
 }
@@ -235,7 +261,10 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
 {
   const FieldDesc f = c->desc(u);
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
-  if (compute && !(c->flags & FACES_GATHER) && row_kernel_supported(c->n))
+  const bool fused = compute && !(c->flags & FACES_GATHER);
+  if (fused && !(c->flags & FACES_ROWS) && tile_kernel_supported(c->n))
+    CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s), "tile kernel launch");
+  else if (fused && row_kernel_supported(c->n))
     CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
   else
     CUDA_TRY(launch_gather(f, compute, s), "gather kernel launch");

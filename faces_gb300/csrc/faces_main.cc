@@ -16,9 +16,10 @@
 //   --periodic        wrap the rank grid (the reference never wraps)
 //   --messages        v-26 strategy: 26 messages per rank, swapped by buffer
 //   --gather          force the generic one-thread-per-point kernel
+//   --rows            use the register row kernel instead of the tile kernel
 //   --init=ref|int    initial state: gpu/main.cc:18 formula (default) or
 //                     integer values from --seed=S
-//   --chunk=K --tpb=T row-kernel work decomposition
+//   --chunk=K --tpb=T --order=O   work decomposition (faces_set_tuning)
 //   --json            one machine-readable line on stderr
 #include <cuda_runtime.h>
 
@@ -61,7 +62,7 @@ void cuda_check(cudaError_t e, const char *what)
 int main(int argc, char *argv[])
 {
   unsigned flags = 0;
-  int init = 0, chunk = 0, tpb = 0;
+  int init = 0, chunk = 0, tpb = 0, order = -1;
   bool json = false;
   unsigned long long seed = 1;
   for (int a = 1; a < argc; a++) {
@@ -69,12 +70,14 @@ int main(int argc, char *argv[])
     if (s == "--periodic") flags |= FACES_PERIODIC;
     else if (s == "--messages") flags |= FACES_MESSAGES;
     else if (s == "--gather") flags |= FACES_GATHER;
+    else if (s == "--rows") flags |= FACES_ROWS;
     else if (s == "--json") json = true;
     else if (s == "--init=ref") init = 0;
     else if (s == "--init=int") init = 1;
     else if (s.rfind("--seed=", 0) == 0) seed = std::strtoull(s.c_str() + 7, nullptr, 10);
     else if (s.rfind("--chunk=", 0) == 0) chunk = std::atoi(s.c_str() + 8);
     else if (s.rfind("--tpb=", 0) == 0) tpb = std::atoi(s.c_str() + 6);
+    else if (s.rfind("--order=", 0) == 0) order = std::atoi(s.c_str() + 8);
     else {
       std::fprintf(stderr, "unknown option %s\n", argv[a]);
       return 2;
@@ -114,7 +117,7 @@ int main(int argc, char *argv[])
     std::cout << (k + 1) << ": ";
     faces_ctx *faces = nullptr;
     TRY(faces_create(&faces, lx, ly, lz, mx, my, mz, n, flags));
-    if (chunk > 0 || tpb > 0) TRY(faces_set_tuning(faces, chunk, tpb));
+    if (chunk > 0 || tpb > 0 || order >= 0) TRY(faces_set_tuning(faces, chunk, tpb, order));
     std::cout << "Initialized Faces: " << mx << " x " << my << " x " << mz << " elements of order " << n - 1
               << " on " << lx << " x " << ly << " x " << lz << " tasks" << std::endl;
     for (int j = 0; j <= niel; j++) {

@@ -16,6 +16,12 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s);
 cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s);
 cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 
+// shared-memory tile step (tiles.cu): chunk (plan.chunk) must be 1, 2, 4 or 8
+bool tile_kernel_supported(int n);
+int tile_default_chunk(int n);
+size_t tile_smem_bytes(int n, int chunk);
+cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);
+
 // Closed-form check of a field after `nshares` shares of a known initial
 // state (init: 0 = reference formula, 1 = integer seed) with the relative
 // error rule of gpu/main.cc:39-105.  Pass 1 (target = 0) raises rank_max[r]

@@ -32,6 +32,7 @@ struct RowPlan {
   int ty, tz;     // tile rows in y and z (m, or m+1 with a virtual top tile)
   long ntiles;    // nranks * tz * ty * nchunks
   int tiles_per_block;
+  int order;      // tile kernel: 0 grid-stride over tiles, 1 contiguous range per block
 };
 
 FACES_HD int nbr_of(const FieldDesc &f, int r, int dir) { return f.nbr[r * 27 + dir]; }
@@ -114,6 +115,7 @@ FACES_HD RowPlan make_row_plan(const FieldDesc &f, int chunk, int tiles_per_bloc
   if (tpb * tt > 256) tpb = 256 / tt;
   if (tpb > 15) tpb = 15;  // named barriers 1..15
   p.tiles_per_block = tpb;
+  p.order = 0;
   return p;
 }
 
@@ -124,14 +126,45 @@ struct TileCoords {
   bool hi_x;  // last chunk takes the extra seam step with element mx
 };
 
-FACES_HD TileCoords tile_coords(const FieldDesc &f, const RowPlan &p, long tile)
+// Mixed-radix position of a tile, (chunk, jy, jz, rank) with radices
+// (nchunks, ty, tz, nranks): a block walks its tiles by adding a constant
+// step to a cursor, without dividing per tile.
+struct TileCursor {
+  int c, jy, jz, r;
+};
+
+FACES_HD TileCursor cursor_of(const RowPlan &p, long tile)
+{
+  TileCursor u;
+  long q = tile;
+  u.c = (int)(q % p.nchunks); q /= p.nchunks;
+  u.jy = (int)(q % p.ty); q /= p.ty;
+  u.jz = (int)(q % p.tz); q /= p.tz;
+  u.r = (int)q;
+  return u;
+}
+
+FACES_HD void cursor_add(const RowPlan &p, TileCursor &a, const TileCursor &d)
+{
+  a.c += d.c;
+  int carry = a.c >= p.nchunks;
+  if (carry) a.c -= p.nchunks;
+  a.jy += d.jy + carry;
+  carry = a.jy >= p.ty;
+  if (carry) a.jy -= p.ty;
+  a.jz += d.jz + carry;
+  carry = a.jz >= p.tz;
+  if (carry) a.jz -= p.tz;
+  a.r += d.r + carry;
+}
+
+FACES_HD TileCoords coords_of(const FieldDesc &f, const RowPlan &p, const TileCursor &u)
 {
   TileCoords t;
-  long q = tile;
-  t.c = (int)(q % p.nchunks); q /= p.nchunks;
-  t.jy = (int)(q % p.ty); q /= p.ty;
-  t.jz = (int)(q % p.tz); q /= p.tz;
-  t.r = (int)q;
+  t.c = u.c;
+  t.jy = u.jy;
+  t.jz = u.jz;
+  t.r = u.r;
   t.jx0 = t.c * p.chunk;
   t.jx1 = t.jx0 + p.chunk < f.m[0] ? t.jx0 + p.chunk : f.m[0];
   // direct mode: a virtual top tile exists only where no upper rank owns the
@@ -140,6 +173,11 @@ FACES_HD TileCoords tile_coords(const FieldDesc &f, const RowPlan &p, long tile)
            (t.jz == f.m[2] && f.mode != kMessages && nbr_of(f, t.r, dir_index(0, 0, 1)) >= 0);
   t.hi_x = (t.c == p.nchunks - 1) && (f.mode == kMessages || nbr_of(f, t.r, dir_index(1, 0, 0)) < 0);
   return t;
+}
+
+FACES_HD TileCoords tile_coords(const FieldDesc &f, const RowPlan &p, long tile)
+{
+  return coords_of(f, p, cursor_of(p, tile));
 }
 
 struct SlotSetup {

@@ -48,6 +48,8 @@ extern "C" {
                                it one owner sums each shared point across
                                ranks in place (same values, no messages). */
 #define FACES_GATHER 0x4u   /* force the generic one-thread-per-point kernel */
+#define FACES_ROWS 0x8u     /* use the register row kernel instead of the
+                               shared-memory tile kernel */
 
 typedef struct faces_ctx faces_ctx;
 
@@ -104,9 +106,12 @@ int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long se
  * (host; may equal u_in).  Synchronous.  Pinned host memory is fastest. */
 int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int compute, int nshares, void *stream);
 
-/* Work decomposition of the row kernel: elements per x-chunk (<= 0: default)
- * and tiles per thread block (<= 0: default). */
-int faces_set_tuning(faces_ctx *ctx, int chunk, int tiles_per_block);
+/* Work decomposition: elements per x-chunk (<= 0: default; the tile kernel
+ * rounds down to 1, 2, 4 or 8), width (<= 0: default): tiles per thread
+ * block for the row kernel, resident blocks per SM for the tile kernel, and
+ * the tile kernel's order (< 0: default, 0: blocks stride over the tiles,
+ * 1: each block takes a contiguous range of x-chunks). */
+int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);

@@ -566,19 +566,44 @@ static void v26_step(const geo *o, double *u, int compute, msgs *mb)
     /* inner (gpu/v-26-messages/Faces.cc:301-376): groups strictly inside the
      * subdomain; every copy is local */
     if (compute) {
-#pragma omp parallel for schedule(static)
-      for (int gz = 1; gz < G[2]; gz++)
-        for (int gy = 1; gy < G[1]; gy++)
-          for (int gx = 1; gx < G[0]; gx++) {
-            if (gx % nm1 && gy % nm1 && gz % nm1) continue;
-            const int gp[3] = {gx, gy, gz};
-            gcop c;
-            int nl;
-            v26_gather(o, ur, r, mb, gp, &c, &nl);
-            const double s = tree_sum(&c);
-            for (int bz = 0; bz < c.cnt[2]; bz++)
-              for (int by = 0; by < c.cnt[1]; by++)
-                for (int bx = 0; bx < c.cnt[0]; bx++) *c.p[bz][by][bx] = s;
+      /* element loops as the reference's fused inner kernel: element
+       * (jx,jy,jz) owns its points with i_a in [0, n-2] that lie on a seam
+       * with a lower element (i_a = 0, j_a > 0); points on the subdomain
+       * boundary (i_a = 0, j_a = 0) are left to the unpack */
+      const int n = o->n;
+      const long s3 = o->s[3], s4 = o->s[4], s5 = o->s[5];
+      const long ox = -s3 + nm1, oy = -s4 + (long)nm1 * n, oz = -s5 + (long)nm1 * n * n;
+#pragma omp parallel for collapse(2) schedule(static)
+      for (int jz = 0; jz < o->m[2]; jz++)
+        for (int jy = 0; jy < o->m[1]; jy++)
+          for (int jx = 0; jx < o->m[0]; jx++) {
+            double *e = ur + jx * s3 + jy * s4 + jz * s5;
+            const int lx = jx > 0 ? 0 : 1, ly = jy > 0 ? 0 : 1, lz = jz > 0 ? 0 : 1;
+            for (int iz = lz; iz < nm1; iz++)
+              for (int iy = ly; iy < nm1; iy++) {
+                /* a row with iy, iz off the seams only has its ix = 0 point */
+                const int xend = (iy && iz) ? (lx == 0 ? 1 : 0) : nm1;
+                for (int ix = lx; ix < xend; ix++) {
+                  double *p = e + ix + (long)iy * n + (long)iz * n * n;
+                  const int cx = ix == 0 ? 2 : 1, cy = iy == 0 ? 2 : 1, cz = iz == 0 ? 2 : 1;
+                  double sy[2];
+                  for (int bz = 0; bz < cz; bz++) {
+                    double sx[2];
+                    for (int by = 0; by < cy; by++) {
+                      const double *q = p + (bz ? oz : 0) + (by ? oy : 0);
+                      sx[by] = (cx == 2) ? q[0] + q[ox] : q[0];
+                    }
+                    sy[bz] = (cy == 2) ? sx[0] + sx[1] : sx[0];
+                  }
+                  const double s = (cz == 2) ? sy[0] + sy[1] : sy[0];
+                  for (int bz = 0; bz < cz; bz++)
+                    for (int by = 0; by < cy; by++) {
+                      double *q = p + (bz ? oz : 0) + (by ? oy : 0);
+                      q[0] = s;
+                      if (cx == 2) q[ox] = s;
+                    }
+                }
+              }
           }
     }
     /* exchange is the direction-keyed swap in recv_buf(); unpack-add

@@ -10,7 +10,7 @@ OUT = os.path.join(HERE, "_build", "librows_emu.so")
 def build() -> str:
     src = os.path.join(HERE, "rows_emu.cc")
     csrc = os.path.join(ROOT, "faces_gb300", "csrc")
-    deps = [src] + [os.path.join(csrc, f) for f in ("geom.cuh", "rows_setup.cuh", "tables.h")]
+    deps = [src] + [os.path.join(csrc, f) for f in ("geom.cuh", "rows_setup.cuh", "tables.h", "tile_ops.cuh")]
     if os.path.exists(OUT) and all(os.path.getmtime(d) <= os.path.getmtime(OUT) for d in deps):
         return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)

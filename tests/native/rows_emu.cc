@@ -6,6 +6,7 @@
 // every pointer stays inside the field or the message buffers and that no
 // field point is written more than once per share.  The message mode's pack
 // is replayed from region(d) as the pack kernel does.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -14,6 +15,7 @@
 #include "geom.cuh"
 #include "rows_setup.cuh"
 #include "tables.h"
+#include "tile_ops.cuh"
 
 using namespace faces;
 
@@ -25,6 +27,7 @@ struct Ctx {
   std::vector<unsigned char> wcount;
   std::string err;
   bool ok = true;
+  long regular_tiles = 0, all_tiles = 0;
 };
 
 bool in_field(const Ctx &c, const double *p, long len)
@@ -169,7 +172,186 @@ void run_tile(Ctx &c, const RowPlan &p, long tile)
   }
 }
 
+// one tile of the shared-memory tile kernel: copy in, groups, copy out -- the
+// same functions the kernel's threads call, run one unit at a time
+// concurrency model: every tile of a launch reads the field as it was at the
+// launch (snapshot), and inside a tile every group / pass item reads the
+// staged cells as they were before the phase -- a read of a cell that
+// another tile or item writes then changes the result
+const double *g_snap = nullptr;  // field snapshot (same layout as c.u0)
+
+static const double *snap_of(const Ctx &c, const double *g)
+{
+  if (g_snap && g >= c.u0 && g < c.u1) return g_snap + (g - c.u0);
+  return g;
+}
+
+// run one phase item by item against a snapshot of the stage: each item
+// reads the pre-phase cells and its writes are applied afterwards
+template <class F>
+static bool phase_concurrent(std::vector<double> &sm, long items, F item, std::string &err)
+{
+  const std::vector<double> before(sm);
+  std::vector<double> out(sm);
+  std::vector<unsigned char> owner(sm.size(), 0);
+  for (long i = 0; i < items; i++) {
+    std::vector<double> work(before);
+    item(work.data(), i);
+    for (size_t j = 0; j < sm.size(); j++)
+      if (std::memcmp(&work[j], &before[j], sizeof(double)) != 0) {
+        if (owner[j]++) { err = "staged cell written by two items"; return false; }
+        out[j] = work[j];
+      }
+  }
+  sm = out;
+  return true;
+}
+
+void run_tile_smem(Ctx &c, const RowPlan &p, long tile, int K, std::vector<RowMeta> &prev, long &prev_tile)
+{
+  const FieldDesc &f = c.f;
+  const int n = f.n, NN = n * n;
+  const TileCoords t = tile_coords(f, p, tile);
+  if (t.skip) return;
+  const int nk = t.jx1 - t.jx0;
+  const bool hi_x = t.hi_x;
+  std::vector<RowMeta> meta(NN);
+  for (int r = 0; r < NN; r++) row_meta(f, t, r, meta[r]);
+  // the kernel reuses the previous chunk's metadata: it must equal the fresh one
+  if (prev_tile == tile - 1 && t.c > 0) {
+    for (int r = 0; r < NN; r++) {
+      RowMeta m;
+      tile_row_meta(f, t, true, prev.data(), r, m);
+      if (m.rd != meta[r].rd || m.lo != meta[r].lo || m.hi != meta[r].hi || m.es != meta[r].es ||
+          m.flags != meta[r].flags) {
+        bad(c, "reused row metadata differs from the fresh one", tile, r % n, r / n, 0);
+        return;
+      }
+    }
+  }
+  prev = meta;
+  prev_tile = tile;
+  const long stage = tile_stage_doubles(n, K);
+  std::vector<double> sm(stage, -12345.0);
+  double *buf = sm.data(), *locol = buf + (long)K * NN * smem_row_stride(n), *hicol = locol + NN;
+  auto in_smem = [&](const double *q, int len) { return q >= sm.data() && q + len <= sm.data() + stage; };
+  const int NP = pieces_per_row(n), PW = piece_doubles(n), RS = smem_row_stride(n);
+  // copy in: the end columns, then every slot (r, p) for every element
+  for (int r = 0; r < NN; r++) {
+    const RowMeta &m = meta[r];
+    if (m.flags & kLoOk) {
+      if (!in_any(c, m.lo, 1)) { bad(c, "lo end outside buffers", tile, r, 0, 0); return; }
+      locol[r] = *snap_of(c, m.lo);
+    }
+    if (m.flags & kHiOk) {
+      if (!in_any(c, m.hi, 1)) { bad(c, "hi end outside buffers", tile, r, 0, 0); return; }
+      hicol[r] = *snap_of(c, m.hi);
+    }
+  }
+  for (int sl = 0; sl < NN * NP; sl++) {
+    const int r = sl / NP, pc = sl % NP;
+    const RowMeta &m = meta[r];
+    if (!(m.flags & kRowValid) || !piece_needed(n, m.flags, pc)) continue;
+    for (int k = 0; k < nk; k++) {
+      Move mv;
+      slot_move(n, m, r, pc, t.jx0, k, buf, mv);
+      if (!in_any(c, mv.g, mv.len)) { bad(c, "tile copy-in outside buffers", tile, r, pc, k); return; }
+      if (!in_smem(mv.s, mv.len) || mv.s + mv.len > locol) { bad(c, "tile copy-in outside its stage", tile, r, pc, k); return; }
+      if (mv.len == 2 && (((uintptr_t)mv.g) & 15)) { bad(c, "16-byte copy-in misaligned", tile, r, pc, k); return; }
+      if (mv.len == 2 && (((char *)mv.s - (char *)sm.data()) & 15)) { bad(c, "16-byte smem slot misaligned", tile, r, pc, k); return; }
+      for (int q = 0; q < mv.len; q++) mv.s[q] = snap_of(c, mv.g)[q];
+    }
+  }
+  bool regular = true;
+  for (int r = 0; r < NN; r++) regular = regular && row_regular(meta[r].flags, hi_x);
+  c.regular_tiles += regular;
+  c.all_tiles++;
+  std::string perr;
+  const long off_buf = buf - sm.data(), off_lo = locol - sm.data(), off_hi = hicol - sm.data();
+  if (regular) {
+    // three dense passes, each item against the pre-pass cells
+    for (int pass = 0; pass < 3 && c.ok; pass++) {
+      const long items = pass == 0 ? xpass_items(n, nk, hi_x) : yzpass_items(n, nk, hi_x);
+      const bool ok = phase_concurrent(sm, items, [&](double *w, long i) {
+        if (pass == 0) xpass_item(n, nk, w + off_buf, w + off_lo, w + off_hi, (int)i);
+        else yzpass_item(n, nk, hi_x, pass, w + off_buf, w + off_lo, w + off_hi, (int)i);
+      }, perr);
+      if (!ok) { bad(c, perr.c_str(), tile, pass, 0, 0); return; }
+    }
+  } else {
+    const bool ok = phase_concurrent(sm, tile_groups(n, nk, hi_x), [&](double *w, long g) {
+      tile_group(n, nk, meta.data(), w + off_buf, w + off_lo, w + off_hi, g);
+    }, perr);
+    if (!ok) { bad(c, perr.c_str(), tile, 0, 0, 0); return; }
+  }
+  // copy out
+  for (int r = 0; r < NN; r++)
+    if (meta[r].flags & kLoWritable) write(c, const_cast<double *>(meta[r].lo), locol[r], tile, r, 0, -1);
+  for (int sl = 0; sl < NN * NP; sl++) {
+    const int r = sl / NP, pc = sl % NP;
+    const RowMeta &m = meta[r];
+    if (!(m.flags & kRowWritable) || !piece_needed(n, m.flags, pc)) continue;
+    for (int k = 0; k < nk; k++) {
+      Move mv;
+      slot_move(n, m, r, pc, t.jx0, k, buf, mv);
+      const int len = slot_out_len(n, nk, hi_x, pc, k);
+      for (int q = 0; q < len; q++) write(c, const_cast<double *>(mv.g) + q, mv.s[q], tile, r, pc, k);
+      if (!c.ok) return;
+    }
+  }
+  (void)PW; (void)RS;
+}
+
 }  // namespace
+
+extern "C" int tiles_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int messages,
+                             int K, double *u, int nsteps, char *err, int errlen, long *regular)
+{
+  Ctx c;
+  FieldDesc &f = c.f;
+  f.n = n;
+  f.m[0] = mx; f.m[1] = my; f.m[2] = mz;
+  f.L[0] = lx; f.L[1] = ly; f.L[2] = lz;
+  f.periodic = periodic;
+  f.mode = messages ? kMessages : kDirect;
+  f.nranks = lx * ly * lz;
+  f.sjy = (long)n * n * n * mx;
+  f.sjz = jz_stride(n, mx, my);
+  f.R = f.sjz * mz;
+  f.u = u;
+  std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
+  std::vector<long> off;
+  long mtot = messages ? message_offsets(f, nbr, off) : 0;
+  if (!messages) off.assign(nbr.size(), -1);
+  std::vector<double> msg(mtot > 0 ? mtot : 1, 0.0);
+  f.nbr = nbr.data();
+  f.msg_off = off.data();
+  f.msg = messages ? msg.data() : nullptr;
+  c.u0 = u;
+  c.u1 = u + f.R * f.nranks;
+  c.m0 = messages ? msg.data() : nullptr;
+  c.m1 = messages ? msg.data() + mtot : nullptr;
+  const RowPlan p = make_row_plan(f, K, 0);
+  std::vector<RowMeta> prev;
+  long prev_tile = -2;
+  std::vector<double> snap;
+  for (int step = 0; step < nsteps && c.ok; step++) {
+    c.wcount.assign(f.R * f.nranks, 0);
+    if (messages) pack(f);
+    snap.assign(u, u + f.R * f.nranks);
+    g_snap = snap.data();
+    // tiles in reverse order too: any order must give the same field
+    for (long tile = 0; tile < p.ntiles && c.ok; tile++)
+      run_tile_smem(c, p, (step % 2) ? p.ntiles - 1 - tile : tile, tile_instance_k(p.chunk), prev, prev_tile);
+  }
+  g_snap = nullptr;
+  if (regular) { regular[0] = c.regular_tiles; regular[1] = c.all_tiles; }
+  if (!c.ok) {
+    snprintf(err, errlen, "%s", c.err.c_str());
+    return -1;
+  }
+  return 0;
+}
 
 extern "C" int rows_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int messages,
                             int chunk, int tiles_per_block, double *u, int nsteps, char *err, int errlen)

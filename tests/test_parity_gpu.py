@@ -17,8 +17,9 @@ if not torch.cuda.is_available():
     pytest.skip("no CUDA device", allow_module_level=True)
 
 
-def run_gpu(F, s, *, periodic, messages, gather=False, init="int", seed=5, nsteps=2, compute=True):
-    f = F.Faces(s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n, periodic=periodic, messages=messages, gather=gather)
+def run_gpu(F, s, *, periodic, messages, gather=False, rows=False, init="int", seed=5, nsteps=2, compute=True):
+    f = F.Faces(s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n, periodic=periodic, messages=messages, gather=gather,
+                rows=rows)
     u = f.field()
     if init == "int":
         f.init_int(u, seed)
@@ -53,11 +54,13 @@ SHAPES = [
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
 @pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
-def test_rows_bit_exact(oracle, faces_lib, shape, periodic, messages):
+@pytest.mark.parametrize("kernel", ["tiles", "rows"])
+def test_step_bit_exact(oracle, faces_lib, shape, periodic, messages, kernel):
     O, F = oracle, faces_lib
     s = O.Shape(*shape, periodic=periodic)
     for init in ("int", "ref"):
-        u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, init=init, nsteps=3)
+        u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, rows=kernel == "rows", init=init,
+                                   nsteps=3)
         ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
         assert np.array_equal(u_init, ref0), "device init differs from the host formula"
         exp = O.groups_share(s, ref0.copy(), True, 3)
@@ -96,15 +99,36 @@ def test_mugs_bit_exact_single_rank(oracle, faces_lib):
     assert np.array_equal(out, O.mugs_share(s, O.init_ref(s), True, 4))
 
 
-@pytest.mark.parametrize("chunk", [1, 2, 3, 5])
-def test_chunking(oracle, faces_lib, chunk):
+@pytest.mark.parametrize("chunk", [1, 2, 3, 5, 8])
+@pytest.mark.parametrize("kernel", ["tiles", "rows"])
+def test_chunking(oracle, faces_lib, chunk, kernel):
     O, F = oracle, faces_lib
     for periodic, messages in itertools.product([False, True], [False, True]):
         s = O.Shape(2, 1, 1, 7, 2, 2, 5, periodic=periodic)
-        f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages)
-        f.set_tuning(chunk=chunk, tiles_per_block=1 + chunk % 3)
+        f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages,
+                    rows=kernel == "rows")
+        f.set_tuning(chunk=chunk, width=1 + chunk % 3, order=chunk % 2)
         u = f.field()
         f.init_ref(u)
         f.share_n(u, 2)
         torch.cuda.synchronize()
         assert np.array_equal(u.cpu().numpy(), O.groups_share(s, O.init_ref(s), True, 2))
+
+
+@pytest.mark.parametrize("kernel", ["tiles", "rows"])
+def test_large_field_properties(oracle, faces_lib, kernel):
+    """The benchmark's 48^3 n=8 periodic field: too large for the oracle in a
+    test, so check size-independent properties on the device: the closed
+    form after several shares, and direct mode == message mode bit for bit."""
+    F = faces_lib
+    outs = []
+    for messages in (False, True):
+        f = F.Faces(1, 1, 1, 48, 48, 48, 8, periodic=True, messages=messages, rows=kernel == "rows")
+        u = f.field()
+        f.init_int(u, 1)
+        f.share_n(u, 6)
+        chk = f.check(u, init="int", seed=1, nshares=6)
+        assert chk.passed and chk.maxrel == 0.0
+        outs.append(u)
+        f.close()
+    assert torch.equal(outs[0], outs[1])
