@@ -115,7 +115,11 @@ void replan(faces_ctx &c)
     k = k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1;
     while (k > 1 && tile_smem_bytes(c.n, k) > 110 * 1024) k /= 2;
     c.tplan = make_row_plan(f, k, 0);
-    c.tplan.order = c.order >= 0 ? c.order : 0;
+    c.tplan.order = c.order >= 0 ? (c.order % 16) : 2;
+    // order 2 units: chunks per unit (tuning value order = 2 + 16*u), default
+    // half a column
+    const int uc = c.order >= 16 ? c.order / 16 : (c.tplan.nchunks + 1) / 2;
+    c.tplan.unit_chunks = uc < 1 ? 1 : uc;
     // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved
     // per block) and 2048 threads of 256-thread blocks
     int fit = (int)((228 * 1024) / (tile_smem_bytes(c.n, k) + 1024));
@@ -242,7 +246,7 @@ int faces_field_free(double *u)
 int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
 {
   if (int rc = check_ctx(c)) return rc;
-  if (order > 1) return fail(FACES_EINVAL, "order = %d: -1 (default), 0 or 1", order);
+  if (order % 16 > 2) return fail(FACES_EINVAL, "order = %d: -1 (default), 0, 1, or 2 + 16*chunks_per_unit", order);
   c->chunk = chunk > 0 ? chunk : 0;
   c->tpb = width > 0 ? width : 0;
   c->order = order;

@@ -32,7 +32,9 @@ struct RowPlan {
   int ty, tz;     // tile rows in y and z (m, or m+1 with a virtual top tile)
   long ntiles;    // nranks * tz * ty * nchunks
   int tiles_per_block;
-  int order;      // tile kernel: 0 grid-stride over tiles, 1 contiguous range per block
+  int order;      // tile kernel: 0 grid-stride over tiles, 1 contiguous range per
+                  // block, 2 grid-stride over units of unit_chunks chunks of a column
+  int unit_chunks;
 };
 
 FACES_HD int nbr_of(const FieldDesc &f, int r, int dir) { return f.nbr[r * 27 + dir]; }
@@ -116,6 +118,7 @@ FACES_HD RowPlan make_row_plan(const FieldDesc &f, int chunk, int tiles_per_bloc
   if (tpb > 15) tpb = 15;  // named barriers 1..15
   p.tiles_per_block = tpb;
   p.order = 0;
+  p.unit_chunks = 1;
   return p;
 }
 

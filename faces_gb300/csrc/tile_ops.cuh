@@ -89,6 +89,52 @@ FACES_HD void tile_row_meta(const FieldDesc &f, const TileCoords &t, bool follow
   }
 }
 
+// Per-slot column state: a thread owns the same slots (row r, piece pc) in
+// every tile, and a row's source (pointer to its element-0 copy, element
+// stride, flags) changes only with the column (rank, jy, jz).
+struct SlotCol {
+  const double *rd;
+  int es;
+  unsigned fl;  // kRowValid | kRowWritable | kInterior
+};
+
+FACES_HD SlotCol slot_col(const FieldDesc &f, const TileCoords &t, int r)
+{
+  const int n = f.n, sy = r % n, sz = r / n;
+  SlotSetup ss;
+  slot_setup(f, t, sy, sz, n, ss);
+  SlotCol c;
+  c.rd = ss.rd;
+  c.es = (int)ss.es;
+  c.fl = (ss.valid ? kRowValid : 0u) | (ss.writable ? kRowWritable : 0u) |
+         ((sy >= 1 && sy <= n - 2 && sz >= 1 && sz <= n - 2) ? kInterior : 0u);
+  return c;
+}
+
+// x ends of row r in tile t: inside a column the previous chunk's last point
+// (from the column state), at the column's ends the neighbours' (full setup,
+// once per column end); returns the row's flags
+FACES_HD unsigned row_ends(const FieldDesc &f, const TileCoords &t, const SlotCol &c, int r, const double *&lo,
+                           const double *&hi)
+{
+  const int n = f.n;
+  bool lo_w = false;
+  lo = hi = nullptr;
+  if (t.c > 0 && !t.hi_x) {
+    if (c.fl & kRowValid) {
+      lo = c.rd + (long)(t.jx0 - 1) * c.es + (n - 1);
+      lo_w = (c.fl & kRowWritable) != 0;
+    }
+  } else {
+    SlotSetup ss;
+    slot_setup(f, t, r % n, r / n, n, ss);
+    lo = ss.lo;
+    lo_w = ss.lo && ss.lo_w;
+    hi = t.hi_x ? ss.hi : nullptr;
+  }
+  return c.fl | (lo ? kLoOk : 0u) | (lo_w ? kLoWritable : 0u) | (hi ? kHiOk : 0u);
+}
+
 // Copies in and out.  Thread-owned slots (r, p) -- staged row r, piece p --
 // repeat over the tile's elements k with fixed strides, so no index is
 // divided per copy.  Interior rows move only their first and last piece:
@@ -182,11 +228,11 @@ FACES_HD void group_point(int n, int nk, long g, int &k, int &ix, int &iy, int &
 // k at ix, or the received x-upper end for the virtual element) and, on an x
 // seam, the lower copy (element k-1 at n-1, or the x-lower end for k = 0).
 template <bool SX>
-FACES_HD void x_level(int n, int nk, const RowMeta *meta, double *buf, double *locol, double *hicol, int k, int ix,
+FACES_HD void x_level(int n, int nk, const unsigned *rflags, double *buf, double *locol, double *hicol, int k, int ix,
                       int r, double *&pu, bool &ou, double *&pl, bool &ol, double &v, bool &present, int &cnt)
 {
   const int NN = n * n, RS = smem_row_stride(n);
-  const unsigned fl = meta[r].flags;
+  const unsigned fl = rflags[r];
   if (k == nk) { pu = hicol + r; ou = (fl & kHiOk) != 0; }
   else { pu = buf + (k * NN + r) * RS + ix; ou = (fl & kRowValid) != 0; }
   double vu = ou ? *pu : 0.0;
@@ -208,7 +254,7 @@ FACES_HD void x_level(int n, int nk, const RowMeta *meta, double *buf, double *l
 // sum of one group: x pairs, then y pairs, then z pairs over the copies that
 // exist, written to every staged copy
 template <bool SX, bool SY, bool SZ>
-FACES_HD void group_sum(int n, int nk, const RowMeta *meta, double *buf, double *locol, double *hicol, int k, int ix,
+FACES_HD void group_sum(int n, int nk, const unsigned *rflags, double *buf, double *locol, double *hicol, int k, int ix,
                         int iy, int iz)
 {
   double *pu[2][2], *pl[2][2];
@@ -225,7 +271,7 @@ FACES_HD void group_sum(int n, int nk, const RowMeta *meta, double *buf, double 
       pu[bz][by] = pl[bz][by] = nullptr;
       if ((!SY && by == 0) || (!SZ && bz == 0)) continue;
       const int r = (by ? iy : n - 1) + n * (bz ? iz : n - 1);
-      x_level<SX>(n, nk, meta, buf, locol, hicol, k, ix, r, pu[bz][by], ou[bz][by], pl[bz][by], ol[bz][by],
+      x_level<SX>(n, nk, rflags, buf, locol, hicol, k, ix, r, pu[bz][by], ou[bz][by], pl[bz][by], ol[bz][by],
                   v[bz][by], pr[bz][by], cnt);
     }
   if (cnt < 2) return;
@@ -247,27 +293,27 @@ FACES_HD void group_sum(int n, int nk, const RowMeta *meta, double *buf, double 
     }
 }
 
-FACES_HD void tile_group_at(int n, int nk, const RowMeta *meta, double *buf, double *locol, double *hicol, int k,
+FACES_HD void tile_group_at(int n, int nk, const unsigned *rflags, double *buf, double *locol, double *hicol, int k,
                             int ix, int iy, int iz)
 {
   const int pat = (ix == 0 ? 1 : 0) | (iy == 0 ? 2 : 0) | (iz == 0 ? 4 : 0);
   switch (pat) {
-    case 1: group_sum<true, false, false>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 2: group_sum<false, true, false>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 4: group_sum<false, false, true>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 3: group_sum<true, true, false>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 5: group_sum<true, false, true>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 6: group_sum<false, true, true>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
-    case 7: group_sum<true, true, true>(n, nk, meta, buf, locol, hicol, k, ix, iy, iz); break;
+    case 1: group_sum<true, false, false>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 2: group_sum<false, true, false>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 4: group_sum<false, false, true>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 3: group_sum<true, true, false>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 5: group_sum<true, false, true>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 6: group_sum<false, true, true>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
+    case 7: group_sum<true, true, true>(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz); break;
     default: break;
   }
 }
 
-FACES_HD void tile_group(int n, int nk, const RowMeta *meta, double *buf, double *locol, double *hicol, long g)
+FACES_HD void tile_group(int n, int nk, const unsigned *rflags, double *buf, double *locol, double *hicol, long g)
 {
   int k, ix, iy, iz;
   group_point(n, nk, g, k, ix, iy, iz);
-  tile_group_at(n, nk, meta, buf, locol, hicol, k, ix, iy, iz);
+  tile_group_at(n, nk, rflags, buf, locol, hicol, k, ix, iy, iz);
 }
 
 struct TileSmemLayout {
@@ -309,10 +355,9 @@ FACES_HD bool row_regular(unsigned flags, bool hi_x)
 // between element k-1 (or the lower end) and element k (or the upper end)
 FACES_HD int xpass_items(int n, int nk, bool hi_x) { return (nk + (hi_x ? 1 : 0)) * n * n; }
 
-FACES_HD void xpass_item(int n, int nk, double *buf, double *locol, double *hicol, int i)
+FACES_HD void xpass_at(int n, int nk, double *buf, double *locol, double *hicol, int k, int r)
 {
   const int NN = n * n, RS = smem_row_stride(n);
-  const int r = i % NN, k = i / NN;
   double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (n - 1);
   double *hi = k == nk ? hicol + r : buf + (k * NN + r) * RS;
   const double s = *lo + *hi;
@@ -320,36 +365,45 @@ FACES_HD void xpass_item(int n, int nk, double *buf, double *locol, double *hico
   *hi = s;
 }
 
+FACES_HD void xpass_item(int n, int nk, double *buf, double *locol, double *hicol, int i)
+{
+  xpass_at(n, nk, buf, locol, hicol, i / (n * n), i % (n * n));
+}
+
 // y pass (axis 1) and z pass (axis 2): item (o, c) pairs the lower row
 // (index n-1 on the axis) with the upper row (index 0) -- o is the row index
-// on the other axis -- at staged column c: c = 0 the lower end column,
-// c = 1 + k*n + x point x of element k, c = 1 + nk*n the upper end column
-// (with hi_x only)
+// on the other axis -- at staged column c: c < nk*n is point c%n of element
+// c/n, c = nk*n the lower end column, c = nk*n+1 the upper end column (with
+// hi_x only)
 FACES_HD int yz_span(int n, int nk, bool hi_x) { return nk * n + 1 + (hi_x ? 1 : 0); }
 FACES_HD int yzpass_items(int n, int nk, bool hi_x) { return n * yz_span(n, nk, hi_x); }
 
-FACES_HD void yzpass_item(int n, int nk, bool hi_x, int axis, double *buf, double *locol, double *hicol, int i)
+FACES_HD void yzpass_at(int n, int nk, int axis, double *buf, double *locol, double *hicol, int o, int c)
 {
   const int NN = n * n, RS = smem_row_stride(n);
-  const int span = yz_span(n, nk, hi_x);
-  const int o = i / span, c = i - o * span;
   const int r_lo = axis == 1 ? (n - 1) + n * o : o + n * (n - 1);
   const int r_hi = axis == 1 ? n * o : o;
   double *a, *b;
-  if (c == 0) {
-    a = locol + r_lo;
-    b = locol + r_hi;
-  } else if (c == 1 + nk * n) {
-    a = hicol + r_lo;
-    b = hicol + r_hi;
-  } else {
-    const int q = c - 1, k = q / n, x = q - k * n;
+  if (c < nk * n) {
+    const int k = c / n, x = c - k * n;
     a = buf + (k * NN + r_lo) * RS + x;
     b = buf + (k * NN + r_hi) * RS + x;
+  } else if (c == nk * n) {
+    a = locol + r_lo;
+    b = locol + r_hi;
+  } else {
+    a = hicol + r_lo;
+    b = hicol + r_hi;
   }
   const double s = *a + *b;
   *a = s;
   *b = s;
+}
+
+FACES_HD void yzpass_item(int n, int nk, bool hi_x, int axis, double *buf, double *locol, double *hicol, int i)
+{
+  const int span = yz_span(n, nk, hi_x);
+  yzpass_at(n, nk, axis, buf, locol, hicol, i / span, i % span);
 }
 
 }  // namespace faces

@@ -31,166 +31,249 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int W>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(W) : "memory"); }
 
-struct TileState {
-  long tile;
-  int jx0, nk;
-  int hi_x;
-  int regular;
+struct ColKey {
+  int r, jy, jz;
+  bool skip, has_hi;
 };
 
-// issue the copies of tile `tile` into stage (meta, data); every thread works
-// out the metadata of the rows it copies, so no barrier is needed here
-template <int N, int K>
-__device__ __forceinline__ void stage_in(const FieldDesc &f, const RowPlan &p, const TileCursor &cu, long tile,
-                                         bool follow, const RowMeta *prev, TileState *ts, RowMeta *meta,
-                                         double *data)
+// the sequence of tiles one block processes
+struct TileWalk {
+  TileCursor u;   // current tile
+  long t, t1;     // orders 0/1: tile index and end
+  long v, nv;     // order 2: unit index and count
+  int c1;         // order 2: end chunk of the unit
+  bool done;
+};
+
+__device__ __forceinline__ void walk_unit(const RowPlan &p, TileWalk &w)
+{
+  // unit v: chunk group q = v / columns, column = v % columns
+  const long ncol = p.ntiles / p.nchunks;
+  const long q = w.v / ncol, column = w.v - q * ncol;
+  const int c0 = (int)q * p.unit_chunks;
+  w.c1 = min(c0 + p.unit_chunks, p.nchunks);
+  w.u = cursor_of(p, column * p.nchunks + c0);
+}
+
+__device__ __forceinline__ void walk_begin(const RowPlan &p, TileWalk &w)
+{
+  w.done = false;
+  if (p.order == 2) {
+    const long ncol = p.ntiles / p.nchunks;
+    w.nv = ncol * ((p.nchunks + p.unit_chunks - 1) / p.unit_chunks);
+    w.v = blockIdx.x;
+    if (w.v >= w.nv) { w.done = true; return; }
+    walk_unit(p, w);
+  } else if (p.order == 1) {
+    w.t = p.ntiles * blockIdx.x / gridDim.x;
+    w.t1 = p.ntiles * (blockIdx.x + 1) / gridDim.x;
+    if (w.t >= w.t1) { w.done = true; return; }
+    w.u = cursor_of(p, w.t);
+  } else {
+    w.t = blockIdx.x;
+    w.t1 = p.ntiles;
+    if (w.t >= w.t1) { w.done = true; return; }
+    w.u = cursor_of(p, w.t);
+  }
+}
+
+__device__ __forceinline__ void walk_next(const RowPlan &p, TileWalk &w)
+{
+  if (p.order == 2) {
+    if (w.u.c + 1 < w.c1) {
+      w.u.c++;
+      return;
+    }
+    w.v += gridDim.x;
+    if (w.v >= w.nv) { w.done = true; return; }
+    walk_unit(p, w);
+  } else if (p.order == 1) {
+    if (++w.t >= w.t1) { w.done = true; return; }
+    const TileCursor one{1, 0, 0, 0};
+    cursor_add(p, w.u, one);
+  } else {
+    w.t += gridDim.x;
+    if (w.t >= w.t1) { w.done = true; return; }
+    w.u = cursor_of(p, w.t);
+  }
+}
+
+__device__ __forceinline__ TileCoords coords_from(const RowPlan &p, const FieldDesc &f, const TileCursor &u,
+                                                  const ColKey &ck)
+{
+  TileCoords t;
+  t.c = u.c;
+  t.jy = u.jy;
+  t.jz = u.jz;
+  t.r = u.r;
+  t.jx0 = u.c * p.chunk;
+  t.jx1 = t.jx0 + p.chunk < f.m[0] ? t.jx0 + p.chunk : f.m[0];
+  t.skip = ck.skip;
+  t.hi_x = ck.has_hi && u.c == p.nchunks - 1;
+  return t;
+}
+
+// Stage one tile: per-slot column state (recomputed when the column changes),
+// the row flags and x ends (one thread per row), and the cp.async copies.
+template <int N, int K, int SPT>
+__device__ __forceinline__ void stage_tile(const FieldDesc &f, const RowPlan &p, const TileCursor &u, ColKey &ck,
+                                           bool &have_col, SlotCol (&col)[SPT], double *data, unsigned *rfl,
+                                           double **lop, SlotCol *rinfo, int4 *tinfo)
 {
   constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
-  const TileCoords t = coords_of(f, p, cu);
-  const int nk = t.skip ? 0 : t.jx1 - t.jx0;
-  if (threadIdx.x == 0) {
-    ts->tile = tile;
-    ts->jx0 = t.jx0;
-    ts->nk = nk;
-    ts->hi_x = (!t.skip && t.hi_x) ? 1 : 0;
-    ts->regular = 0;
+  const bool newcol = !have_col || ck.r != u.r || ck.jy != u.jy || ck.jz != u.jz;
+  if (newcol) {
+    ck.r = u.r;
+    ck.jy = u.jy;
+    ck.jz = u.jz;
+    ck.skip = (u.jy == f.m[1] && f.mode != kMessages && nbr_of(f, u.r, dir_index(0, 1, 0)) >= 0) ||
+              (u.jz == f.m[2] && f.mode != kMessages && nbr_of(f, u.r, dir_index(0, 0, 1)) >= 0);
+    ck.has_hi = f.mode == kMessages || nbr_of(f, u.r, dir_index(1, 0, 0)) < 0;
+    have_col = true;
   }
-  if (nk > 0) {
-    double *buf = data, *locol = data + K * NN * RS, *hicol = locol + NN;
-    for (int sl = threadIdx.x; sl < NN * NP; sl += blockDim.x) {
-      const int r = sl / NP, pc = sl % NP;
-      RowMeta m;
-      tile_row_meta(f, t, follow, prev, r, m);
-      if (pc == 0) {
-        meta[r] = m;
-        if (m.flags & kLoOk) cp_async(locol + r, m.lo, 1);
-        if (m.flags & kHiOk) cp_async(hicol + r, m.hi, 1);
-      }
-      if (!(m.flags & kRowValid) || !piece_needed(N, m.flags, pc)) continue;
-      Move mv;
-      slot_move(N, m, r, pc, t.jx0, 0, buf, mv);
-      const double *g = mv.g;
-      double *sp = mv.s;
-      for (int k = 0; k < nk; k++, g += m.es, sp += NN * RS) cp_async(sp, g, PW);
+  const TileCoords t = coords_from(p, f, u, ck);
+  const int nk = t.skip ? 0 : t.jx1 - t.jx0;
+  if (threadIdx.x == 0) *tinfo = make_int4(t.jx0, nk, t.hi_x ? 1 : 0, 0);
+  double *buf = data, *locol = data + K * NN * RS, *hicol = locol + NN;
+#pragma unroll
+  for (int j = 0; j < SPT; j++) {
+    const int sl = threadIdx.x + j * 256;
+    if (sl >= NN * NP) continue;
+    const int r = sl / NP, pc = sl - (sl / NP) * NP;
+    if (newcol) col[j] = slot_col(f, t, r);
+    if (nk == 0) continue;
+    const SlotCol &c = col[j];
+    if (pc == 0) {
+      const double *lo, *hi;
+      rfl[r] = row_ends(f, t, c, r, lo, hi);
+      lop[r] = const_cast<double *>(lo);
+      rinfo[r] = c;
+      if (lo) cp_async(locol + r, lo, 1);
+      if (hi) cp_async(hicol + r, hi, 1);
     }
+    if (!(c.fl & kRowValid) || !piece_needed(N, c.fl, pc)) continue;
+    const double *g = c.rd + (long)t.jx0 * c.es + pc * PW;
+    double *sp = buf + r * RS + pc * PW;
+    for (int k = 0; k < nk; k++, g += c.es, sp += NN * RS) cp_async(sp, g, PW);
   }
   cp_commit();
 }
 
-template <int N, int K>
-__device__ __forceinline__ void stage_out(const TileState &ts, const RowMeta *meta, double *data)
-{
-  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
-  double *buf = data, *locol = data + K * NN * RS;
-  for (int r = threadIdx.x; r < NN; r += blockDim.x) {
-    const RowMeta &m = meta[r];
-    if (m.flags & kLoWritable) *const_cast<double *>(m.lo) = locol[r];
-  }
-  for (int sl = threadIdx.x; sl < NN * NP; sl += blockDim.x) {
-    const int r = sl / NP, pc = sl % NP;
-    const RowMeta &m = meta[r];
-    if (!(m.flags & kRowWritable) || !piece_needed(N, m.flags, pc)) continue;
-    Move mv;
-    slot_move(N, m, r, pc, ts.jx0, 0, buf, mv);
-    double *g = const_cast<double *>(mv.g);
-    const double *sp = mv.s;
-    for (int k = 0; k < ts.nk; k++, g += m.es, sp += NN * RS) {
-      const int len = slot_out_len(N, ts.nk, ts.hi_x != 0, pc, k);
-      if (PW == 2 && len == 2) *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(sp);
-      else if (len >= 1) *g = *sp;
-    }
-  }
-}
-
 }  // namespace
 
-// stage layout (doubles): NS data stages, then NS*N*N RowMeta, then NS TileState
+// shared memory layout, in doubles from a 16-byte aligned base: NS data
+// stages, NS*N*N x-lower pointers, NS*N*N row flags (unsigned), NS tile
+// infos (int4: jx0, nk, hi_x); every region starts on 16 bytes
 template <int N, int K>
 __host__ __device__ constexpr int tile_stage_size() { return K * N * N * smem_row_stride(N) + 2 * N * N; }
+__host__ __device__ constexpr int round2(int d) { return (d + 1) & ~1; }
+__host__ __device__ constexpr int lop_doubles(int n, int ns) { return round2(ns * n * n); }
+__host__ __device__ constexpr int rfl_doubles(int n, int ns) { return (ns * n * n + 3) / 4 * 2; }
+__host__ __device__ constexpr int rinfo_doubles(int n, int ns) { return ns * n * n * 2; }
 
 template <int N, int K, int NS>
-__global__ void __launch_bounds__(256) tile_kernel(FieldDesc f, RowPlan p)
+__global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
 {
-  constexpr int NN = N * N, RS = smem_row_stride(N);
+  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int SPT = (NN * NP + 255) / 256;
   constexpr int stage = tile_stage_size<N, K>();
   extern __shared__ __align__(16) double sm[];
-  RowMeta *meta_base = reinterpret_cast<RowMeta *>(sm + NS * stage);
-  TileState *ts_base = reinterpret_cast<TileState *>(meta_base + NS * NN);
+  static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
+  double **lop_base = reinterpret_cast<double **>(sm + NS * stage);
+  unsigned *rfl_base = reinterpret_cast<unsigned *>(sm + NS * stage + lop_doubles(N, NS));
+  SlotCol *rinfo_base = reinterpret_cast<SlotCol *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS));
+  int4 *tinfo = reinterpret_cast<int4 *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS) +
+                                         rinfo_doubles(N, NS));
+  static_assert(sizeof(SlotCol) == 16, "row info is two doubles");
 
-  // the block's tiles: a contiguous range (consecutive x-chunks of a
-  // column: the row metadata carries over) or every gridDim.x-th tile
-  long t0, t1, step;
-  if (p.order == 1) {
-    t0 = p.ntiles * blockIdx.x / gridDim.x;
-    t1 = p.ntiles * (blockIdx.x + 1) / gridDim.x;
-    step = 1;
-  } else {
-    t0 = blockIdx.x;
-    t1 = p.ntiles;
-    step = gridDim.x;
-  }
-  if (t0 >= t1) return;
-  const TileCursor dstep = cursor_of(p, step);
-  TileCursor nc = cursor_of(p, t0);  // next tile to stage
-  long nt = t0;
-  // prologue: the first NS-1 tiles in flight
+  // The block's tiles, walked by a TileWalk: a contiguous range (order 1),
+  // every gridDim.x-th tile (order 0), or every gridDim.x-th unit of
+  // unit_chunks consecutive chunks of one column, units ordered chunk group
+  // first so that the blocks running at one time hold neighbouring columns
+  // (order 2).  Consecutive tiles of one column share their rows' sources.
+  TileWalk nw;  // next tile to stage
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;  // staged tiles not yet summed
+  ColKey ck{};
+  bool have_col = false;
+  SlotCol col[SPT];  // the staged column's row sources, per owned slot
 #pragma unroll
   for (int j = 0; j < NS - 1; j++) {
-    if (nt < t1) {
-      // fresh metadata: the prologue has no barrier between its stages
-      stage_in<N, K>(f, p, nc, nt, false, nullptr, ts_base + j, meta_base + j * NN, sm + j * stage);
-      cursor_add(p, nc, dstep);
-      nt += step;
+    if (!nw.done) {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + j * stage, rfl_base + j * NN, lop_base + j * NN,
+                            rinfo_base + j * NN, tinfo + j);
+      walk_next(p, nw);
+      inflight++;
     } else {
       cp_commit();
     }
   }
-  // the loop reads row metadata and tile state that other threads wrote in
-  // the prologue
+  // the loop reads row flags and tile infos other threads wrote
   __syncthreads();
   int s = 0;
-  for (long t = t0; t < t1; t += step) {
+  for (; inflight > 0; inflight--) {
     cp_wait<NS - 2>();
-    // tile t is staged; the block agrees whether it is regular
-    const RowMeta *meta = meta_base + s * NN;
+    const unsigned *rfl = rfl_base + s * NN;
+    const int4 ti = tinfo[s];
+    const int nk = ti.y;
+    const bool hx = ti.z != 0;
     bool ok = true;
-    if ((int)threadIdx.x < NN) ok = row_regular(meta[threadIdx.x].flags, ts_base[s].hi_x != 0);
+    if ((int)threadIdx.x < NN) ok = row_regular(rfl[threadIdx.x], hx);
     const int regular = __syncthreads_and(ok);
     // the stage of the previous tile is free again: the next prefetch goes there
     const int sn = (s + NS - 1) % NS;
-    if (nt < t1) {
-      // contiguous order: nt-1 is staged in the stage before sn
-      const bool follow = p.order == 1 && nc.c != 0;
-      stage_in<N, K>(f, p, nc, nt, follow, meta_base + (sn - 1 + NS) % NS * NN, ts_base + sn,
-                     meta_base + sn * NN, sm + sn * stage);
-      cursor_add(p, nc, dstep);
-      nt += step;
+    if (!nw.done) {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + sn * stage, rfl_base + sn * NN, lop_base + sn * NN,
+                            rinfo_base + sn * NN, tinfo + sn);
+      walk_next(p, nw);
+      inflight++;
     } else {
       cp_commit();
     }
-    const TileState cur = ts_base[s];
     double *buf = sm + s * stage, *locol = buf + K * NN * RS, *hicol = locol + NN;
-    if (cur.nk > 0) {
-      const bool hx = cur.hi_x != 0;
+    if (nk > 0) {
       if (regular) {
-        const int nx = xpass_items(N, cur.nk, hx);
-        for (int i = threadIdx.x; i < nx; i += blockDim.x) xpass_item(N, cur.nk, buf, locol, hicol, i);
+        const int nx = (nk + (hx ? 1 : 0)) * NN;
+        for (int i = threadIdx.x; i < nx; i += blockDim.x) xpass_at(N, nk, buf, locol, hicol, i / NN, i % NN);
         __syncthreads();
-        const int ny = yzpass_items(N, cur.nk, hx);
-        for (int i = threadIdx.x; i < ny; i += blockDim.x) yzpass_item(N, cur.nk, hx, 1, buf, locol, hicol, i);
+        const int span = nk * N + 1 + (hx ? 1 : 0);
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int o = warp; o < N; o += 8)
+          for (int c = lane; c < span; c += 32) yzpass_at(N, nk, 1, buf, locol, hicol, o, c);
         __syncthreads();
-        for (int i = threadIdx.x; i < ny; i += blockDim.x) yzpass_item(N, cur.nk, hx, 2, buf, locol, hicol, i);
+        for (int o = warp; o < N; o += 8)
+          for (int c = lane; c < span; c += 32) yzpass_at(N, nk, 2, buf, locol, hicol, o, c);
       } else {
-        const int groups = (int)tile_groups(N, cur.nk, hx);
+        const int groups = (int)tile_groups(N, nk, hx);
         for (int g = threadIdx.x; g < groups; g += blockDim.x) {
           int k, ix, iy, iz;
-          group_point(N, cur.nk, g, k, ix, iy, iz);
-          tile_group_at(N, cur.nk, meta, buf, locol, hicol, k, ix, iy, iz);
+          group_point(N, nk, g, k, ix, iy, iz);
+          tile_group_at(N, nk, rfl, buf, locol, hicol, k, ix, iy, iz);
         }
       }
     }
     __syncthreads();
-    if (cur.nk > 0) stage_out<N, K>(cur, meta, buf);
+    if (nk > 0) {
+      // copy out: the changed rows, and the x-lower end where it is local
+      if ((int)threadIdx.x < NN && (rfl[threadIdx.x] & kLoWritable))
+        *(lop_base + s * NN)[threadIdx.x] = locol[threadIdx.x];
+#pragma unroll
+      for (int j = 0; j < SPT; j++) {
+        const int sl = threadIdx.x + j * 256;
+        if (sl >= NN * NP) continue;
+        const int r = sl / NP, pc = sl - (sl / NP) * NP;
+        const SlotCol c = rinfo_base[s * NN + r];
+        if (!(c.fl & kRowWritable) || !piece_needed(N, c.fl, pc)) continue;
+        double *g = const_cast<double *>(c.rd) + (long)ti.x * c.es + pc * PW;
+        const double *sp = buf + r * RS + pc * PW;
+        for (int k = 0; k < nk; k++, g += c.es, sp += NN * RS) {
+          const int len = slot_out_len(N, nk, hx, pc, k);
+          if (PW == 2 && len == 2) *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(sp);
+          else if (len >= 1) *g = *sp;
+        }
+      }
+    }
     s = (s + 1) % NS;
   }
 }
@@ -213,8 +296,10 @@ constexpr int kTileStages = 3;
 size_t tile_smem_bytes(int n, int chunk)
 {
   const int K = tile_instance_k(chunk);
-  return sizeof(double) * kTileStages * tile_stage_doubles(n, K) + kTileStages * sizeof(RowMeta) * n * n +
-         kTileStages * sizeof(TileState);
+  // data stages, x-lower pointers, row flags, tile infos (see tile_kernel)
+  return sizeof(double) * (kTileStages * tile_stage_doubles(n, K) + lop_doubles(n, kTileStages) +
+                           rfl_doubles(n, kTileStages) + rinfo_doubles(n, kTileStages)) +
+         sizeof(int4) * kTileStages;
 }
 
 template <int N, int K>

@@ -109,8 +109,9 @@ int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int comput
 /* Work decomposition: elements per x-chunk (<= 0: default; the tile kernel
  * rounds down to 1, 2, 4 or 8), width (<= 0: default): tiles per thread
  * block for the row kernel, resident blocks per SM for the tile kernel, and
- * the tile kernel's order (< 0: default, 0: blocks stride over the tiles,
- * 1: each block takes a contiguous range of x-chunks). */
+ * the tile kernel's order (< 0: default = 2, 0: blocks stride over the tiles,
+ * 1: each block takes a contiguous range of x-chunks, 2 + 16*u: blocks stride
+ * over units of u consecutive x-chunks of a column, u = 0 half a column). */
 int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 
 /* Kernel launches one share enqueues with the current settings. */

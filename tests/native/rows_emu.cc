@@ -217,6 +217,17 @@ void run_tile_smem(Ctx &c, const RowPlan &p, long tile, int K, std::vector<RowMe
   const bool hi_x = t.hi_x;
   std::vector<RowMeta> meta(NN);
   for (int r = 0; r < NN; r++) row_meta(f, t, r, meta[r]);
+  // the tile kernel's per-slot column state and x ends must reproduce the
+  // full setup of every row
+  for (int r = 0; r < NN; r++) {
+    const SlotCol sc = slot_col(f, t, r);
+    const double *lo, *hi;
+    const unsigned fl = row_ends(f, t, sc, r, lo, hi);
+    if (sc.rd != meta[r].rd || sc.es != meta[r].es || fl != meta[r].flags || lo != meta[r].lo || hi != meta[r].hi) {
+      bad(c, "slot column state differs from the full row setup", tile, r % n, r / n, 0);
+      return;
+    }
+  }
   // the kernel reuses the previous chunk's metadata: it must equal the fresh one
   if (prev_tile == tile - 1 && t.c > 0) {
     for (int r = 0; r < NN; r++) {
@@ -268,6 +279,8 @@ void run_tile_smem(Ctx &c, const RowPlan &p, long tile, int K, std::vector<RowMe
   c.all_tiles++;
   std::string perr;
   const long off_buf = buf - sm.data(), off_lo = locol - sm.data(), off_hi = hicol - sm.data();
+  std::vector<unsigned> rflags(NN);
+  for (int r = 0; r < NN; r++) rflags[r] = meta[r].flags;
   if (regular) {
     // three dense passes, each item against the pre-pass cells
     for (int pass = 0; pass < 3 && c.ok; pass++) {
@@ -280,7 +293,7 @@ void run_tile_smem(Ctx &c, const RowPlan &p, long tile, int K, std::vector<RowMe
     }
   } else {
     const bool ok = phase_concurrent(sm, tile_groups(n, nk, hi_x), [&](double *w, long g) {
-      tile_group(n, nk, meta.data(), w + off_buf, w + off_lo, w + off_hi, g);
+      tile_group(n, nk, rflags.data(), w + off_buf, w + off_lo, w + off_hi, g);
     }, perr);
     if (!ok) { bad(c, perr.c_str(), tile, 0, 0, 0); return; }
   }

@@ -107,7 +107,7 @@ def test_chunking(oracle, faces_lib, chunk, kernel):
         s = O.Shape(2, 1, 1, 7, 2, 2, 5, periodic=periodic)
         f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages,
                     rows=kernel == "rows")
-        f.set_tuning(chunk=chunk, width=1 + chunk % 3, order=chunk % 2)
+        f.set_tuning(chunk=chunk, width=1 + chunk % 3, order=[0, 1, 2, 2 + 16][chunk % 4])
         u = f.field()
         f.init_ref(u)
         f.share_n(u, 2)
