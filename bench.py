@@ -49,7 +49,7 @@ E2E_SHARES = 100  # ni of the configuration (nk=1 nj=1 ni=100)
 # shares; here the re-init runs INSIDE the timed region and counts against
 # the result.
 RESEED_EVERY = 100
-KERNEL_NAME = "faces::tile_kernel<8,8>"
+KERNEL_NAME = "faces::tile_kernel<8,4,3>"
 L2_BYTES = 126 * 2 ** 20
 
 
@@ -326,10 +326,11 @@ def run_reference(args) -> dict | None:
     if rank != 0:
         return None
     cb = cpu_baseline(budget_s=min(60.0, 2.0 + 0.05 * max(args.steps, 1)), min_steps=max(1, min(args.steps, 3)))
+    done = int(cb["sample"].split()[0])
     from oracle import oracle as O
     s = O.Shape(**SHAPE, periodic=PERIODIC)
     return {
-        "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": world, "steps": done,
         "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: integer-valued FP64 uniform in [0,2^20) (splitmix64 seed 1)",
