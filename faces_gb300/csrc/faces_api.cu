@@ -52,6 +52,9 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 }  // namespace
 
+// error text for faces_last_error() from the other translation units
+void faces_internal_set_error(const char *msg) { g_err = msg; }
+
 struct faces_ctx {
   int L[3], m[3], n;
   unsigned flags;

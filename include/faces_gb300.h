@@ -120,6 +120,27 @@ int faces_launches_per_share(const faces_ctx *ctx, int compute);
 /* Message of the last failed call on this thread ("" if none). */
 const char *faces_last_error(void);
 
+/* Doubles in the device array faces_share_static works in (32 MiB). */
+#define FACES_STATIC_SCRATCH_DOUBLES (4L << 20)
+
+/* One message-mode share (FACES_MESSAGES) of the field u -- lx*ly*lz ranks of
+ * mx*my*mz elements of n^3 points in the layout above -- that allocates no
+ * device memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc, such as applications that give all device memory
+ * to their own pool at start-up, and latency-critical loops that cannot take
+ * the device-wide synchronisation cudaMalloc and cudaFree imply.  Its working
+ * memory (neighbour table, message offsets, the 26 messages of every rank)
+ * lives in one file-scope device array of FACES_STATIC_SCRATCH_DOUBLES
+ * doubles, held by every GPU that loads the library until the process
+ * exits; a field whose tables and messages do not fit is rejected with
+ * FACES_EINVAL.  The array's device address is taken on the first call on
+ * each device, so make that first call before any stream capture.  All calls
+ * share the array and each rewrites what it reads; calls that overlap on the
+ * GPU race.  flags: FACES_PERIODIC or 0.  Stream-ordered like faces_share;
+ * the result equals faces_share with FACES_MESSAGES bit for bit. */
+int faces_share_static(double *u, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags,
+                       int compute, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
