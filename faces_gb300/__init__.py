@@ -67,9 +67,23 @@ def lib() -> ctypes.CDLL:
     L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
     L.faces_last_error.restype = ctypes.c_char_p
+    ip = ctypes.POINTER(c_int)
+    L.faces_batch_create.argtypes = [ctypes.POINTER(vp)]
+    L.faces_batch_add.argtypes = [vp, dp] + [c_int] * 7 + [c_uint, ip]
+    L.faces_batch_commit.argtypes = [vp]
+    L.faces_batch_share.argtypes = [vp, c_int, vp]
+    L.faces_batch_share_n.argtypes = [vp, c_int, c_int, vp]
+    L.faces_batch_share_each.argtypes = [vp, c_int, vp]
+    L.faces_batch_tune.argtypes = [vp, c_int, c_int]
+    L.faces_batch_autotune.argtypes = [vp, c_int, vp]
+    L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip]
+    L.faces_batch_destroy.argtypes = [vp]
     for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
                  "faces_share", "faces_share_n", "faces_init_ref", "faces_init_int", "faces_check",
-                 "faces_run_host", "faces_set_tuning", "faces_launches_per_share"):
+                 "faces_run_host", "faces_set_tuning", "faces_launches_per_share", "faces_batch_create",
+                 "faces_batch_add", "faces_batch_commit", "faces_batch_share", "faces_batch_share_n",
+                 "faces_batch_share_each", "faces_batch_tune", "faces_batch_autotune", "faces_batch_info",
+                 "faces_batch_destroy"):
         getattr(L, name).restype = c_int
     _lib = L
     return L
@@ -228,3 +242,72 @@ class Faces:
 
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))
+
+
+class Batch:
+    """Many independent fields advanced together (no counterpart in the
+    reference, which runs one field per process: gpu/main.cc:169-180).
+
+    add() the fields (each a Faces shape and a device field of that shape),
+    commit(), then share() advances every field by one share with one
+    persistent launch; share_n() replays n shares as one CUDA graph;
+    share_each() is one faces_share per field.  The fields stay owned by
+    the caller and must outlive the batch.
+    """
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _check(lib().faces_batch_create(ctypes.byref(h)))
+        self._h = h
+        self._fields = []
+
+    def add(self, faces: Faces, u) -> int:
+        lx, ly, lz, mx, my, mz, n = faces.shape
+        flags = ((PERIODIC if faces.periodic else 0) | (MESSAGES if faces.messages else 0)
+                 | (GATHER if faces.gather else 0) | (ROWS if faces.rows else 0))
+        fid = ctypes.c_int()
+        _check(lib().faces_batch_add(self._h, _ptr(u), lx, ly, lz, mx, my, mz, n, flags, ctypes.byref(fid)))
+        self._fields.append(u)
+        return fid.value
+
+    def commit(self) -> None:
+        _check(lib().faces_batch_commit(self._h))
+
+    def share(self, compute: bool = True, stream=None) -> None:
+        _check(lib().faces_batch_share(self._h, int(compute), _stream(stream)))
+
+    def share_n(self, nshares: int, compute: bool = True, stream=None) -> None:
+        _check(lib().faces_batch_share_n(self._h, int(compute), nshares, _stream(stream)))
+
+    def share_each(self, compute: bool = True, stream=None) -> None:
+        _check(lib().faces_batch_share_each(self._h, int(compute), _stream(stream)))
+
+    def tune(self, unit_div: int = 0, blocks_per_sm: int = 0) -> None:
+        _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm))
+
+    def autotune(self, trials: int = 3, stream=None) -> int:
+        """Keeps the fastest work split; returns the shares it applied to
+        each field of the batched launch (each timed launch is a share)."""
+        return _check(lib().faces_batch_autotune(self._h, trials, _stream(stream)))
+
+    def info(self) -> dict:
+        v = [ctypes.c_int() for _ in range(5)]
+        _check(lib().faces_batch_info(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks"), (x.value for x in v)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().faces_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

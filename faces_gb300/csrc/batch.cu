@@ -1,0 +1,523 @@
+// batch.cu -- many independent fields, one persistent launch per share.
+//
+// A batch holds fields of different shapes (rank grid, mx,my,mz, n).  One
+// launch of batch_kernel advances every field by one share: the work list is
+// every field's element columns cut into units of consecutive x-chunks,
+// listed field by field and, inside a field, chunk group first, so the blocks
+// running at one time hold neighbouring columns of one field.  Each block
+// walks every gridDim.x-th unit through the same 3-stage cp.async pipeline as
+// the single-field tile kernel, switching on each tile's n.  A CUDA graph of
+// several launches replays the steps with one host call.  The plain form --
+// one launch of the single-field kernel per field -- is kept for comparison.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/faces_gb300.h"
+#include "ctx.h"
+#include "geom.cuh"
+#include "kernels.cuh"
+#include "rows_setup.cuh"
+#include "tile_ops.cuh"
+#include "tile_steps.cuh"
+
+void faces_internal_set_error(const char *msg);
+
+namespace faces {
+
+using namespace tiledev;
+
+namespace {
+
+// elements per tile for each n: as many as fit a ~20 KB stage, a power of 2
+__host__ __device__ constexpr int bk(int n) { return tile_kmax(n); }
+__host__ __device__ constexpr int bspt(int n) { return (n * n * pieces_per_row(n) + 255) / 256; }
+
+constexpr int kBatchMinN = 2, kBatchMaxN = 10, kBatchStages = 3;
+constexpr int kNNMax = kBatchMaxN * kBatchMaxN;
+
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int stage_of(int n) { return bk(n) * n * n * smem_row_stride(n) + 2 * n * n; }
+__host__ __device__ constexpr int stage_max(int n)
+{
+  return n < kBatchMinN ? 0 : cmax(stage_of(n), stage_max(n - 1));
+}
+__host__ __device__ constexpr int spt_max(int n) { return n < kBatchMinN ? 0 : cmax(bspt(n), spt_max(n - 1)); }
+
+constexpr int kStage = (stage_max(kBatchMaxN) + 1) & ~1;
+constexpr int kSptMax = spt_max(kBatchMaxN);
+
+struct BatchField {
+  FieldDesc f;
+  RowPlan p;
+};
+
+struct BatchUnit {
+  int field, column, c0, c1;
+};
+
+// shared memory: data stages, then per-stage row arrays sized for n = 10
+constexpr long batch_smem_bytes()
+{
+  return sizeof(double) * (long)kBatchStages * kStage + sizeof(double *) * (long)kBatchStages * kNNMax +
+         sizeof(SlotCol) * (long)kBatchStages * kNNMax + sizeof(unsigned) * (long)kBatchStages * kNNMax +
+         sizeof(int4) * kBatchStages;
+}
+
+struct BWalk {
+  int u, c, c1, field;
+  TileCursor cur;
+  bool done;
+};
+
+__device__ __forceinline__ void bwalk_unit(const BatchField *fields, const BatchUnit *units, BWalk &w)
+{
+  const BatchUnit un = units[w.u];
+  w.field = un.field;
+  w.c = un.c0;
+  w.c1 = un.c1;
+  const RowPlan &p = fields[un.field].p;
+  w.cur = cursor_of(p, (long)un.column * p.nchunks + un.c0);
+}
+
+__device__ __forceinline__ void bwalk_next(const BatchField *fields, const BatchUnit *units, int nunits, BWalk &w)
+{
+  if (w.c + 1 < w.c1) {
+    w.c++;
+    w.cur.c++;
+    return;
+  }
+  w.u += gridDim.x;
+  if (w.u >= nunits) {
+    w.done = true;
+    return;
+  }
+  bwalk_unit(fields, units, w);
+}
+
+struct Smem {
+  double *data;
+  double **lop;
+  SlotCol *rinfo;
+  unsigned *rfl;
+  int4 *tinfo;
+};
+
+__device__ __forceinline__ Smem smem_layout(double *sm)
+{
+  static_assert(kStage % 2 == 0, "stages keep 16-byte alignment");
+  static_assert((kBatchStages * kNNMax * sizeof(unsigned)) % 16 == 0, "tile infos stay 16-byte aligned");
+  Smem m;
+  m.data = sm;
+  m.lop = reinterpret_cast<double **>(sm + (long)kBatchStages * kStage);
+  m.rinfo = reinterpret_cast<SlotCol *>(m.lop + kBatchStages * kNNMax);
+  m.rfl = reinterpret_cast<unsigned *>(m.rinfo + kBatchStages * kNNMax);
+  m.tinfo = reinterpret_cast<int4 *>(m.rfl + kBatchStages * kNNMax);
+  return m;
+}
+
+template <int N>
+__device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u, ColKey &ck, bool &have_col,
+                                       SlotCol (&col)[kSptMax], const Smem &m, int st)
+{
+  stage_tile<N, bk(N), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage, m.rfl + st * kNNMax,
+                            m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
+}
+
+// stage tile u of field `field` into stage st; the tile info's z holds
+// hi_x | n << 1 and w the field
+__device__ __forceinline__ void bstage_any(const BatchField *fields, int field, const TileCursor &u, ColKey &ck,
+                                           bool &have_col, SlotCol (&col)[kSptMax], const Smem &m, int st)
+{
+  const BatchField &bf = fields[field];
+  switch (bf.f.n) {
+#define FACES_BSTAGE(NV) \
+  case NV: bstage<NV>(bf, u, ck, have_col, col, m, st); break;
+    FACES_BSTAGE(2) FACES_BSTAGE(3) FACES_BSTAGE(4) FACES_BSTAGE(5) FACES_BSTAGE(6) FACES_BSTAGE(7) FACES_BSTAGE(8)
+    FACES_BSTAGE(9) FACES_BSTAGE(10)
+#undef FACES_BSTAGE
+    default:
+      if (threadIdx.x == 0) m.tinfo[st] = make_int4(0, 0, 0, 0);
+      cp_commit();
+      break;
+  }
+  if (threadIdx.x == 0) {
+    int4 ti = m.tinfo[st];
+    ti.z = (ti.z & 1) | (bf.f.n << 1);
+    ti.w = field;
+    m.tinfo[st] = ti;
+  }
+}
+
+__global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits)
+{
+  extern __shared__ __align__(16) double sm[];
+  const Smem m = smem_layout(sm);
+  BWalk nw;  // next tile to stage
+  nw.u = blockIdx.x;
+  nw.done = nw.u >= nunits;
+  if (nw.done) return;
+  bwalk_unit(fields, units, nw);
+  ColKey ck{};
+  bool have_col = false;
+  int last_field = -1;
+  SlotCol col[kSptMax];
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < kBatchStages - 1; j++) {
+    if (!nw.done) {
+      if (nw.field != last_field) { have_col = false; last_field = nw.field; }
+      bstage_any(fields, nw.field, nw.cur, ck, have_col, col, m, j);
+      bwalk_next(fields, units, nunits, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  __syncthreads();
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<kBatchStages - 2>();
+    const unsigned *rfl = m.rfl + s * kNNMax;
+    const int4 ti = m.tinfo[s];
+    const int nk = ti.y, n = ti.z >> 1;
+    const bool hx = (ti.z & 1) != 0;
+    bool ok = true;
+    if ((int)threadIdx.x < n * n) ok = row_regular(rfl[threadIdx.x], hx);
+    const int regular = __syncthreads_and(ok);
+    const int sn = (s + kBatchStages - 1) % kBatchStages;
+    if (!nw.done) {
+      if (nw.field != last_field) { have_col = false; last_field = nw.field; }
+      bstage_any(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
+      bwalk_next(fields, units, nunits, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = m.data + (long)s * kStage;
+    if (nk > 0) {
+      switch (n) {
+#define FACES_BSUM(NV) \
+  case NV: sum_tile<NV, bk(NV)>(buf, rfl, nk, hx, regular != 0); break;
+        FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
+        FACES_BSUM(9) FACES_BSUM(10)
+#undef FACES_BSUM
+        default: break;
+      }
+    }
+    __syncthreads();
+    if (nk > 0) {
+      switch (n) {
+#define FACES_BSTORE(NV)                                                                                \
+  case NV:                                                                                               \
+    store_tile<NV, bk(NV), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
+    break;
+        FACES_BSTORE(2) FACES_BSTORE(3) FACES_BSTORE(4) FACES_BSTORE(5) FACES_BSTORE(6) FACES_BSTORE(7)
+        FACES_BSTORE(8) FACES_BSTORE(9) FACES_BSTORE(10)
+#undef FACES_BSTORE
+        default: break;
+      }
+    }
+    s = (s + 1) % kBatchStages;
+  }
+}
+
+int fail(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  faces_internal_set_error(buf);
+  return code;
+}
+
+#define CUDA_TRY(call, what)                                                                      \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail(e_ == cudaErrorMemoryAllocation ? FACES_ENOMEM : FACES_ECUDA, "%s: %s", what, \
+                  cudaGetErrorString(e_));                                                        \
+  } while (0)
+
+}  // namespace
+}  // namespace faces
+
+using namespace faces;
+
+struct faces_batch {
+  std::vector<faces_ctx *> ctx;
+  std::vector<double *> u;
+  std::vector<char> fused;  // field runs in the batched kernel
+  bool committed = false;
+  BatchField *d_fields = nullptr;
+  BatchUnit *d_units = nullptr;
+  int nunits = 0;
+  int unit_div = 2;  // units are 1/unit_div of a column's chunks
+  int per_sm = 3;
+  int sms = 0;
+  long grid = 0;
+  cudaStream_t capture = nullptr;
+  std::map<long, cudaGraphExec_t> graphs;  // key: nshares*2 + compute
+  std::vector<BatchField> h_fields;
+};
+
+namespace {
+
+bool batch_eligible(const faces_ctx *c)
+{
+  return c->n >= kBatchMinN && c->n <= kBatchMaxN && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS));
+}
+
+void drop_graphs(faces_batch *b)
+{
+  for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
+}
+
+int build_units(faces_batch *b)
+{
+  // fields in order of n, so that the blocks resident at one time mostly run
+  // the code of one n
+  std::vector<size_t> order;
+  for (size_t i = 0; i < b->h_fields.size(); i++)
+    if (b->fused[i]) order.push_back(i);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t c) { return b->h_fields[a].f.n < b->h_fields[c].f.n; });
+  std::vector<BatchUnit> units;
+  for (size_t i : order) {
+    const RowPlan &p = b->h_fields[i].p;
+    const long ncol = p.ntiles / p.nchunks;
+    const int uc = std::max(1, (p.nchunks + b->unit_div - 1) / b->unit_div);
+    for (int c0 = 0; c0 < p.nchunks; c0 += uc)
+      for (long col = 0; col < ncol; col++) units.push_back({(int)i, (int)col, c0, std::min(c0 + uc, p.nchunks)});
+  }
+  cudaFree(b->d_units);
+  b->d_units = nullptr;
+  b->nunits = (int)units.size();
+  if (!units.empty()) {
+    CUDA_TRY(cudaMalloc(&b->d_units, sizeof(BatchUnit) * units.size()), "faces_batch: work list");
+    CUDA_TRY(cudaMemcpy(b->d_units, units.data(), sizeof(BatchUnit) * units.size(), cudaMemcpyHostToDevice),
+             "faces_batch: work list upload");
+  }
+  b->grid = std::min<long>((long)b->sms * b->per_sm, std::max(1, b->nunits));
+  drop_graphs(b);
+  return FACES_OK;
+}
+
+int launch_batched(faces_batch *b, cudaStream_t s)
+{
+  if (b->nunits == 0) return FACES_OK;
+  batch_kernel<<<(unsigned)b->grid, 256, batch_smem_bytes(), s>>>(b->d_fields, b->d_units, b->nunits);
+  CUDA_TRY(cudaGetLastError(), "batch kernel launch");
+  return FACES_OK;
+}
+
+int check_batch(const faces_batch *b, bool committed)
+{
+  if (!b) return fail(FACES_EINVAL, "null batch");
+  if (committed && !b->committed) return fail(FACES_EINVAL, "batch not committed (faces_batch_commit)");
+  if (!committed && b->committed) return fail(FACES_EINVAL, "batch already committed");
+  return FACES_OK;
+}
+
+// one share of the fields the batched kernel does not take, one launch each
+int share_others(faces_batch *b, int compute, bool all, void *stream)
+{
+  for (size_t i = 0; i < b->ctx.size(); i++)
+    if (all || !b->fused[i] || !compute)
+      if (int rc = faces_share(b->ctx[i], b->u[i], compute, stream)) return rc;
+  return FACES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int faces_batch_create(faces_batch **out)
+{
+  if (!out) return fail(FACES_EINVAL, "null output pointer");
+  faces_batch *b = new (std::nothrow) faces_batch();
+  if (!b) return fail(FACES_ENOMEM, "host allocation failed");
+  int dev = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+    delete b;
+    return fail(FACES_ECUDA, "faces_batch_create: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return FACES_OK;
+}
+
+int faces_batch_add(faces_batch *b, double *u, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags,
+                    int *field_id)
+{
+  if (int rc = check_batch(b, false)) return rc;
+  if (!u || (reinterpret_cast<uintptr_t>(u) & 15u)) return fail(FACES_EALIGN, "field pointer null or not 16-byte aligned");
+  faces_ctx *c = nullptr;
+  if (int rc = faces_create(&c, lx, ly, lz, mx, my, mz, n, flags)) return rc;
+  b->ctx.push_back(c);
+  b->u.push_back(u);
+  if (field_id) *field_id = (int)b->ctx.size() - 1;
+  return FACES_OK;
+}
+
+int faces_batch_commit(faces_batch *b)
+{
+  if (int rc = check_batch(b, false)) return rc;
+  const size_t nf = b->ctx.size();
+  b->h_fields.resize(nf);
+  b->fused.assign(nf, 0);
+  for (size_t i = 0; i < nf; i++) {
+    const faces_ctx *c = b->ctx[i];
+    BatchField bf;
+    bf.f = c->desc(b->u[i]);
+    bf.p = make_row_plan(bf.f, c->n >= kBatchMinN && c->n <= kBatchMaxN ? bk(c->n) : 1, 0);
+    bf.p.order = 2;
+    bf.p.unit_chunks = 1;
+    b->h_fields[i] = bf;
+    b->fused[i] = batch_eligible(c) ? 1 : 0;
+  }
+  if (nf) {
+    CUDA_TRY(cudaMalloc(&b->d_fields, sizeof(BatchField) * nf), "faces_batch: field table");
+    CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * nf, cudaMemcpyHostToDevice),
+             "faces_batch: field table upload");
+  }
+  CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem_bytes()),
+           "faces_batch: shared memory attribute");
+  b->per_sm = std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  CUDA_TRY(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "faces_batch: capture stream");
+  b->committed = true;
+  return build_units(b);
+}
+
+int faces_batch_share(faces_batch *b, int compute, void *stream)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (compute)
+    if (int rc = launch_batched(b, s)) return rc;
+  return share_others(b, compute, false, stream);
+}
+
+int faces_batch_share_n(faces_batch *b, int compute, int nshares, void *stream)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
+  if (nshares == 0) return FACES_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long key = (long)nshares * 2 + (compute ? 1 : 0);
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    // capture nshares steps once; the graph replays them with one call
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "faces_batch: begin capture");
+    int rc = FACES_OK;
+    for (int i = 0; i < nshares && rc == FACES_OK; i++) rc = faces_batch_share(b, compute, b->capture);
+    const cudaError_t e = cudaStreamEndCapture(b->capture, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CUDA_TRY(e, "faces_batch: end capture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e2 = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    CUDA_TRY(e2, "faces_batch: instantiate graph");
+    it = b->graphs.emplace(key, exec).first;
+  }
+  CUDA_TRY(cudaGraphLaunch(it->second, s), "faces_batch: graph launch");
+  return FACES_OK;
+}
+
+int faces_batch_share_each(faces_batch *b, int compute, void *stream)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  return share_others(b, compute, true, stream);
+}
+
+int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  if (unit_div > 0) b->unit_div = unit_div;
+  if (blocks_per_sm > 0) b->per_sm = std::min(blocks_per_sm, std::max(1, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  return build_units(b);
+}
+
+int faces_batch_autotune(faces_batch *b, int trials, void *stream)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  if (trials < 1) trials = 3;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int fit = std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
+  CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
+  float best = 1e30f;
+  int best_div = b->unit_div, best_sm = b->per_sm;
+  int applied = 0;  // shares the timed launches applied to each batched field
+  int rc = FACES_OK;
+  const int divs[] = {1, 2, 4, 8};
+  for (int d : divs) {
+    for (int sm = fit; sm >= std::max(1, fit - 1) && rc == FACES_OK; sm--) {
+      b->unit_div = d;
+      b->per_sm = sm;
+      if ((rc = build_units(b))) break;
+      if (b->nunits == 0) break;
+      if ((rc = launch_batched(b, s))) break;  // warm-up
+      cudaEventRecord(e0, s);
+      for (int t = 0; t < trials && rc == FACES_OK; t++) rc = launch_batched(b, s);
+      cudaEventRecord(e1, s);
+      applied += 1 + trials;
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (rc == FACES_OK && e != cudaSuccess)
+        rc = fail(FACES_ECUDA, "autotune: synchronize: %s", cudaGetErrorString(e));
+      float ms = 0;
+      if (rc == FACES_OK) cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == FACES_OK && ms < best) { best = ms; best_div = d; best_sm = sm; }
+    }
+    if (rc != FACES_OK || b->nunits == 0) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  b->unit_div = best_div;
+  b->per_sm = best_sm;
+  if ((rc = build_units(b))) return rc;
+  return applied;
+}
+
+int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks)
+{
+  if (!b) return fail(FACES_EINVAL, "null batch");
+  int fu = 0;
+  for (char c : b->fused) fu += c;
+  if (fields) *fields = (int)b->ctx.size();
+  if (fused_fields) *fused_fields = fu;
+  if (units) *units = b->nunits;
+  if (unit_div) *unit_div = b->unit_div;
+  if (blocks) *blocks = (int)b->grid;
+  return FACES_OK;
+}
+
+int faces_batch_destroy(faces_batch *b)
+{
+  if (!b) return FACES_OK;
+  drop_graphs(b);
+  if (b->capture) cudaStreamDestroy(b->capture);
+  for (faces_ctx *c : b->ctx) faces_destroy(c);
+  cudaFree(b->d_fields);
+  cudaFree(b->d_units);
+  delete b;
+  return FACES_OK;
+}
+
+}  // extern "C"

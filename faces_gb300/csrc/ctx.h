@@ -1,0 +1,47 @@
+// ctx.h -- the context behind faces_ctx (internal to the library).
+#pragma once
+
+#include <vector>
+
+#include "../../include/faces_gb300.h"
+#include "geom.cuh"
+#include "rows_setup.cuh"
+
+struct faces_ctx {
+  // geometry, flags, device tables and launch plans of one field (all ranks)
+  int L[3], m[3], n;
+  unsigned flags;
+  int nranks;
+  long sjy, sjz, R, total;
+  std::vector<int> nbr;       // [rank*27+dir]
+  std::vector<long> msg_off;  // [rank*27+dir], -1: none
+  long msg_total = 0;
+  int *d_nbr = nullptr;
+  long *d_off = nullptr;
+  double *d_msg = nullptr;
+  unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
+  double *d_field = nullptr;                // faces_run_host's device copy
+  int chunk = 0, tpb = 0, order = -1;
+  int sms = 0;       // multiprocessors of the device
+  faces::RowPlan plan;   // row kernel
+  faces::RowPlan tplan;  // tile kernel
+  long tgrid = 0;    // tile kernel CTAs
+
+  faces::FieldDesc desc(double *u) const
+  {
+    faces::FieldDesc f;
+    f.u = u;
+    f.sjy = sjy; f.sjz = sjz; f.R = R;
+    f.n = n;
+    for (int a = 0; a < 3; a++) { f.m[a] = m[a]; f.L[a] = L[a]; }
+    f.periodic = (flags & FACES_PERIODIC) ? 1 : 0;
+    f.mode = (flags & FACES_MESSAGES) ? faces::kMessages : faces::kDirect;
+    f.nranks = nranks;
+    f.msg = d_msg;
+    f.msg_off = d_off;
+    f.nbr = d_nbr;
+    return f;
+  }
+};
+
+

@@ -18,6 +18,8 @@
 #include "geom.cuh"
 #include "kernels.cuh"
 #include "tables.h"
+#include "ctx.h"
+#include "tile_ops.cuh"
 
 using namespace faces;
 
@@ -55,42 +57,6 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 // error text for faces_last_error() from the other translation units
 void faces_internal_set_error(const char *msg) { g_err = msg; }
 
-struct faces_ctx {
-  int L[3], m[3], n;
-  unsigned flags;
-  int nranks;
-  long sjy, sjz, R, total;
-  std::vector<int> nbr;       // [rank*27+dir]
-  std::vector<long> msg_off;  // [rank*27+dir], -1: none
-  long msg_total = 0;
-  int *d_nbr = nullptr;
-  long *d_off = nullptr;
-  double *d_msg = nullptr;
-  unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
-  double *d_field = nullptr;                // faces_run_host's device copy
-  int chunk = 0, tpb = 0, order = -1;
-  int sms = 0;       // multiprocessors of the device
-  RowPlan plan;      // row kernel
-  RowPlan tplan;     // tile kernel
-  long tgrid = 0;    // tile kernel CTAs
-
-  FieldDesc desc(double *u) const
-  {
-    FieldDesc f;
-    f.u = u;
-    f.sjy = sjy; f.sjz = sjz; f.R = R;
-    f.n = n;
-    for (int a = 0; a < 3; a++) { f.m[a] = m[a]; f.L[a] = L[a]; }
-    f.periodic = (flags & FACES_PERIODIC) ? 1 : 0;
-    f.mode = (flags & FACES_MESSAGES) ? kMessages : kDirect;
-    f.nranks = nranks;
-    f.msg = d_msg;
-    f.msg_off = d_off;
-    f.nbr = d_nbr;
-    return f;
-  }
-};
-
 namespace {
 
 // default x-chunk: whole rows when that already fills the GPU, else split
@@ -113,9 +79,12 @@ void replan(faces_ctx &c)
   const FieldDesc f = c.desc(nullptr);
   c.plan = make_row_plan(f, c.chunk > 0 ? c.chunk : default_chunk(c), c.tpb);
   if (tile_kernel_supported(c.n)) {
-    // the tile kernel is built for 1, 2, 4 or 8 elements per tile
+    // the tile kernel is built for 1, 2, 4, ... tile_kinst_max(n) elements
+    // per tile: a requested chunk rounds down to one of them
     int k = c.chunk > 0 ? c.chunk : tile_default_chunk(c.n);
-    k = k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1;
+    int k2 = 1;
+    while (k2 * 2 <= k && k2 * 2 <= tile_kinst_max(c.n)) k2 *= 2;
+    k = k2;
     while (k > 1 && tile_smem_bytes(c.n, k) > 110 * 1024) k /= 2;
     c.tplan = make_row_plan(f, k, 0);
     c.tplan.order = c.order >= 0 ? (c.order % 16) : 2;

@@ -16,7 +16,7 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s);
 cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s);
 cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 
-// shared-memory tile step (tiles.cu): chunk (plan.chunk) must be 1, 2, 4 or 8
+// shared-memory tile step (tiles.cu): chunk (plan.chunk) at most tile_kinst_max(n)
 bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);
 size_t tile_smem_bytes(int n, int chunk);

@@ -321,9 +321,27 @@ struct TileSmemLayout {
   long doubles;                            // per stage, data part
 };
 
-// the kernel is instantiated for K = 1, 2, 4, 8 elements per tile; a plan
-// whose chunk is smaller (clamped to mx) runs in the next larger instance
-FACES_HD int tile_instance_k(int chunk) { return chunk <= 1 ? 1 : chunk <= 2 ? 2 : chunk <= 4 ? 4 : 8; }
+// Elements per tile by default: as many as fit a ~20 KB stage, rounded down
+// to a power of 2 in [1, 32] (three stages and three resident blocks per SM
+// then fit in shared memory).
+FACES_HD constexpr int tile_kmax(int n)
+{
+  return 20480 / (n * n * smem_row_stride(n) * 8) >= 32 ? 32
+         : 20480 / (n * n * smem_row_stride(n) * 8) >= 16 ? 16
+         : 20480 / (n * n * smem_row_stride(n) * 8) >= 8  ? 8
+         : 20480 / (n * n * smem_row_stride(n) * 8) >= 4  ? 4
+         : 20480 / (n * n * smem_row_stride(n) * 8) >= 2  ? 2
+                                                           : 1;
+}
+
+// the kernel is instantiated for K = 1, 2, 4, ..., tile_kinst_max(n)
+// elements per tile; a plan whose chunk is smaller (clamped to mx) runs in
+// the next larger instance
+FACES_HD constexpr int tile_kinst_max(int n) { return tile_kmax(n) > 8 ? tile_kmax(n) : 8; }
+FACES_HD int tile_instance_k(int chunk)
+{
+  return chunk <= 1 ? 1 : chunk <= 2 ? 2 : chunk <= 4 ? 4 : chunk <= 8 ? 8 : chunk <= 16 ? 16 : 32;
+}
 
 FACES_HD long tile_stage_doubles(int n, int K)
 {

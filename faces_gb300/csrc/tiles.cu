@@ -12,164 +12,11 @@
 #include "kernels.cuh"
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
+#include "tile_steps.cuh"
 
 namespace faces {
 
-namespace {
-
-__device__ __forceinline__ void cp_async(double *dst, const double *src, int len)
-{
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  if (len == 2)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
-}
-
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int W>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(W) : "memory"); }
-
-struct ColKey {
-  int r, jy, jz;
-  bool skip, has_hi;
-};
-
-// the sequence of tiles one block processes
-struct TileWalk {
-  TileCursor u;   // current tile
-  long t, t1;     // orders 0/1: tile index and end
-  long v, nv;     // order 2: unit index and count
-  int c1;         // order 2: end chunk of the unit
-  bool done;
-};
-
-__device__ __forceinline__ void walk_unit(const RowPlan &p, TileWalk &w)
-{
-  // unit v: chunk group q = v / columns, column = v % columns
-  const long ncol = p.ntiles / p.nchunks;
-  const long q = w.v / ncol, column = w.v - q * ncol;
-  const int c0 = (int)q * p.unit_chunks;
-  w.c1 = min(c0 + p.unit_chunks, p.nchunks);
-  w.u = cursor_of(p, column * p.nchunks + c0);
-}
-
-__device__ __forceinline__ void walk_begin(const RowPlan &p, TileWalk &w)
-{
-  w.done = false;
-  if (p.order == 2) {
-    const long ncol = p.ntiles / p.nchunks;
-    w.nv = ncol * ((p.nchunks + p.unit_chunks - 1) / p.unit_chunks);
-    w.v = blockIdx.x;
-    if (w.v >= w.nv) { w.done = true; return; }
-    walk_unit(p, w);
-  } else if (p.order == 1) {
-    w.t = p.ntiles * blockIdx.x / gridDim.x;
-    w.t1 = p.ntiles * (blockIdx.x + 1) / gridDim.x;
-    if (w.t >= w.t1) { w.done = true; return; }
-    w.u = cursor_of(p, w.t);
-  } else {
-    w.t = blockIdx.x;
-    w.t1 = p.ntiles;
-    if (w.t >= w.t1) { w.done = true; return; }
-    w.u = cursor_of(p, w.t);
-  }
-}
-
-__device__ __forceinline__ void walk_next(const RowPlan &p, TileWalk &w)
-{
-  if (p.order == 2) {
-    if (w.u.c + 1 < w.c1) {
-      w.u.c++;
-      return;
-    }
-    w.v += gridDim.x;
-    if (w.v >= w.nv) { w.done = true; return; }
-    walk_unit(p, w);
-  } else if (p.order == 1) {
-    if (++w.t >= w.t1) { w.done = true; return; }
-    const TileCursor one{1, 0, 0, 0};
-    cursor_add(p, w.u, one);
-  } else {
-    w.t += gridDim.x;
-    if (w.t >= w.t1) { w.done = true; return; }
-    w.u = cursor_of(p, w.t);
-  }
-}
-
-__device__ __forceinline__ TileCoords coords_from(const RowPlan &p, const FieldDesc &f, const TileCursor &u,
-                                                  const ColKey &ck)
-{
-  TileCoords t;
-  t.c = u.c;
-  t.jy = u.jy;
-  t.jz = u.jz;
-  t.r = u.r;
-  t.jx0 = u.c * p.chunk;
-  t.jx1 = t.jx0 + p.chunk < f.m[0] ? t.jx0 + p.chunk : f.m[0];
-  t.skip = ck.skip;
-  t.hi_x = ck.has_hi && u.c == p.nchunks - 1;
-  return t;
-}
-
-// Stage one tile: per-slot column state (recomputed when the column changes),
-// the row flags and x ends (one thread per row), and the cp.async copies.
-template <int N, int K, int SPT>
-__device__ __forceinline__ void stage_tile(const FieldDesc &f, const RowPlan &p, const TileCursor &u, ColKey &ck,
-                                           bool &have_col, SlotCol (&col)[SPT], double *data, unsigned *rfl,
-                                           double **lop, SlotCol *rinfo, int4 *tinfo)
-{
-  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
-  const bool newcol = !have_col || ck.r != u.r || ck.jy != u.jy || ck.jz != u.jz;
-  if (newcol) {
-    ck.r = u.r;
-    ck.jy = u.jy;
-    ck.jz = u.jz;
-    ck.skip = (u.jy == f.m[1] && f.mode != kMessages && nbr_of(f, u.r, dir_index(0, 1, 0)) >= 0) ||
-              (u.jz == f.m[2] && f.mode != kMessages && nbr_of(f, u.r, dir_index(0, 0, 1)) >= 0);
-    ck.has_hi = f.mode == kMessages || nbr_of(f, u.r, dir_index(1, 0, 0)) < 0;
-    have_col = true;
-  }
-  const TileCoords t = coords_from(p, f, u, ck);
-  const int nk = t.skip ? 0 : t.jx1 - t.jx0;
-  if (threadIdx.x == 0) *tinfo = make_int4(t.jx0, nk, t.hi_x ? 1 : 0, 0);
-  double *buf = data, *locol = data + K * NN * RS, *hicol = locol + NN;
-#pragma unroll
-  for (int j = 0; j < SPT; j++) {
-    const int sl = threadIdx.x + j * 256;
-    if (sl >= NN * NP) continue;
-    const int r = sl / NP, pc = sl - (sl / NP) * NP;
-    if (newcol) col[j] = slot_col(f, t, r);
-    if (nk == 0) continue;
-    const SlotCol &c = col[j];
-    if (pc == 0) {
-      const double *lo, *hi;
-      rfl[r] = row_ends(f, t, c, r, lo, hi);
-      lop[r] = const_cast<double *>(lo);
-      rinfo[r] = c;
-      if (lo) cp_async(locol + r, lo, 1);
-      if (hi) cp_async(hicol + r, hi, 1);
-    }
-    if (!(c.fl & kRowValid) || !piece_needed(N, c.fl, pc)) continue;
-    const double *g = c.rd + (long)t.jx0 * c.es + pc * PW;
-    double *sp = buf + r * RS + pc * PW;
-    for (int k = 0; k < nk; k++, g += c.es, sp += NN * RS) cp_async(sp, g, PW);
-  }
-  cp_commit();
-}
-
-}  // namespace
-
-// shared memory layout, in doubles from a 16-byte aligned base: NS data
-// stages, NS*N*N x-lower pointers, NS*N*N row flags (unsigned), NS tile
-// infos (int4: jx0, nk, hi_x); every region starts on 16 bytes
-template <int N, int K>
-__host__ __device__ constexpr int tile_stage_size() { return K * N * N * smem_row_stride(N) + 2 * N * N; }
-__host__ __device__ constexpr int round2(int d) { return (d + 1) & ~1; }
-__host__ __device__ constexpr int lop_doubles(int n, int ns) { return round2(ns * n * n); }
-__host__ __device__ constexpr int rfl_doubles(int n, int ns) { return (ns * n * n + 3) / 4 * 2; }
-__host__ __device__ constexpr int rinfo_doubles(int n, int ns) { return ns * n * n * 2; }
+using namespace tiledev;
 
 template <int N, int K, int NS>
 __global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
@@ -231,65 +78,17 @@ __global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
     } else {
       cp_commit();
     }
-    double *buf = sm + s * stage, *locol = buf + K * NN * RS, *hicol = locol + NN;
-    if (nk > 0) {
-      if (regular) {
-        const int nx = (nk + (hx ? 1 : 0)) * NN;
-        for (int i = threadIdx.x; i < nx; i += blockDim.x) xpass_at(N, nk, buf, locol, hicol, i / NN, i % NN);
-        __syncthreads();
-        const int span = nk * N + 1 + (hx ? 1 : 0);
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int o = warp; o < N; o += 8)
-          for (int c = lane; c < span; c += 32) yzpass_at(N, nk, 1, buf, locol, hicol, o, c);
-        __syncthreads();
-        for (int o = warp; o < N; o += 8)
-          for (int c = lane; c < span; c += 32) yzpass_at(N, nk, 2, buf, locol, hicol, o, c);
-      } else {
-        const int groups = (int)tile_groups(N, nk, hx);
-        for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-          int k, ix, iy, iz;
-          group_point(N, nk, g, k, ix, iy, iz);
-          tile_group_at(N, nk, rfl, buf, locol, hicol, k, ix, iy, iz);
-        }
-      }
-    }
+    double *buf = sm + s * stage;
+    if (nk > 0) sum_tile<N, K>(buf, rfl, nk, hx, regular != 0);
     __syncthreads();
-    if (nk > 0) {
-      // copy out: the changed rows, and the x-lower end where it is local
-      if ((int)threadIdx.x < NN && (rfl[threadIdx.x] & kLoWritable))
-        *(lop_base + s * NN)[threadIdx.x] = locol[threadIdx.x];
-#pragma unroll
-      for (int j = 0; j < SPT; j++) {
-        const int sl = threadIdx.x + j * 256;
-        if (sl >= NN * NP) continue;
-        const int r = sl / NP, pc = sl - (sl / NP) * NP;
-        const SlotCol c = rinfo_base[s * NN + r];
-        if (!(c.fl & kRowWritable) || !piece_needed(N, c.fl, pc)) continue;
-        double *g = const_cast<double *>(c.rd) + (long)ti.x * c.es + pc * PW;
-        const double *sp = buf + r * RS + pc * PW;
-        for (int k = 0; k < nk; k++, g += c.es, sp += NN * RS) {
-          const int len = slot_out_len(N, nk, hx, pc, k);
-          if (PW == 2 && len == 2) *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(sp);
-          else if (len >= 1) *g = *sp;
-        }
-      }
-    }
+    if (nk > 0) store_tile<N, K, SPT>(buf, rfl, lop_base + s * NN, rinfo_base + s * NN, ti.x, nk, hx);
     s = (s + 1) % NS;
   }
 }
 
 bool tile_kernel_supported(int n) { return n >= 2 && n <= 12; }
 
-// elements per tile: as many as fit a ~20 KB stage, at least 1 (three
-// stages and three resident blocks per SM then fit in shared memory)
-int tile_default_chunk(int n)
-{
-  const long per_elem = (long)n * n * smem_row_stride(n) * 8;
-  long k = 20480 / per_elem;
-  if (k < 1) k = 1;
-  // the kernel is instantiated for these chunk sizes
-  return k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1;
-}
+int tile_default_chunk(int n) { return tile_kmax(n); }
 
 constexpr int kTileStages = 3;
 
@@ -324,12 +123,19 @@ static cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
 template <int N>
 static cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
 {
-  if (p.chunk > 8) return cudaErrorInvalidValue;
+  constexpr int KM = tile_kinst_max(N);
+  if (p.chunk > KM) return cudaErrorInvalidValue;
   switch (tile_instance_k(p.chunk)) {
     case 1: return launch_tiles_nk<N, 1>(f, p, grid, s);
     case 2: return launch_tiles_nk<N, 2>(f, p, grid, s);
     case 4: return launch_tiles_nk<N, 4>(f, p, grid, s);
     case 8: return launch_tiles_nk<N, 8>(f, p, grid, s);
+    case 16:
+      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, s);
+      return cudaErrorInvalidValue;
+    case 32:
+      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, s);
+      return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }

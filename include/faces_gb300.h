@@ -107,7 +107,7 @@ int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long se
 int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int compute, int nshares, void *stream);
 
 /* Work decomposition: elements per x-chunk (<= 0: default; the tile kernel
- * rounds down to 1, 2, 4 or 8), width (<= 0: default): tiles per thread
+ * rounds down to a power of 2, at most 8, or 16/32 for n <= 5/3), width (<= 0: default): tiles per thread
  * block for the row kernel, resident blocks per SM for the tile kernel, and
  * the tile kernel's order (< 0: default = 2, 0: blocks stride over the tiles,
  * 1: each block takes a contiguous range of x-chunks, 2 + 16*u: blocks stride
@@ -140,6 +140,56 @@ const char *faces_last_error(void);
  * the result equals faces_share with FACES_MESSAGES bit for bit. */
 int faces_share_static(double *u, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags,
                        int compute, void *stream);
+
+/* ---- Batches: many independent fields advanced together ----
+ *
+ * The reference advances one field per process: a Faces object per field
+ * and one share call per step (gpu/main.cc:169-180).  A batch holds any
+ * number of fields of different shapes on one GPU; faces_batch_share
+ * advances all of them by one share, bit for bit as faces_share would, with
+ * one launch of a persistent kernel for the fields it takes (direct mode,
+ * 2 <= n <= 10, compute = 1) and one faces_share per other field. */
+typedef struct faces_batch faces_batch;
+
+int faces_batch_create(faces_batch **b);
+
+/* Adds the field u (device, 16-byte aligned, laid out as for faces_create
+ * with these arguments) and returns its index in *field_id (may be NULL).
+ * Only before faces_batch_commit. */
+int faces_batch_add(faces_batch *b, double *u, int lx, int ly, int lz, int mx, int my, int mz, int n,
+                    unsigned flags, int *field_id);
+
+/* Builds the device work list; the batch is fixed afterwards. */
+int faces_batch_commit(faces_batch *b);
+
+/* One share of every field: one batched launch plus one faces_share per
+ * field the batched kernel does not take.  Stream-ordered. */
+int faces_batch_share(faces_batch *b, int compute, void *stream);
+
+/* nshares shares of every field as one CUDA graph, captured on the first
+ * call for each (nshares, compute) and replayed after.  Stream-ordered. */
+int faces_batch_share_n(faces_batch *b, int compute, int nshares, void *stream);
+
+/* One share of every field, one faces_share call per field (the reference's
+ * pattern; the baseline the batched launch is measured against). */
+int faces_batch_share_each(faces_batch *b, int compute, void *stream);
+
+/* Work list settings: unit_div (units are 1/unit_div of a column's
+ * x-chunks; <= 0 keeps it) and resident blocks per SM (<= 0 keeps it). */
+int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm);
+
+/* Times the batched launch over unit_div in {1,2,4,8} and the resident
+ * blocks per SM that fit, `trials` launches each (after one warm-up), and
+ * keeps the fastest.  Every launch is a share of the fields in the batched
+ * launch (the others are untouched): returns how many shares it applied to
+ * each of them (>= 0), or a negative error code.  Synchronous. */
+int faces_batch_autotune(faces_batch *b, int trials, void *stream);
+
+/* fields, fields in the batched launch, work units, unit_div, blocks of the
+ * batched launch (each may be NULL). */
+int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks);
+
+int faces_batch_destroy(faces_batch *b);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,148 @@
+"""Batches: many fields of different shapes advanced by one persistent launch
+per share must give every field exactly what faces_share gives it alone,
+and what the oracle gives."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+
+# lx ly lz mx my mz n, periodic, messages
+MIX = [
+    ((1, 1, 1, 4, 4, 4, 5), False, False),
+    ((1, 1, 1, 3, 2, 5, 8), True, False),
+    ((1, 1, 1, 1, 1, 1, 3), False, False),
+    ((2, 1, 1, 3, 2, 2, 4), True, False),
+    ((1, 2, 2, 2, 3, 2, 6), False, False),
+    ((3, 3, 3, 2, 2, 2, 6), True, False),
+    ((2, 2, 2, 1, 1, 1, 7), False, False),
+    ((1, 1, 1, 5, 2, 3, 10), True, False),
+    ((1, 1, 1, 9, 2, 2, 2), False, False),
+    ((1, 3, 1, 3, 1, 2, 9), True, False),
+    ((2, 1, 2, 2, 2, 1, 12), False, False),   # n > 10: one faces_share of its own
+    ((2, 1, 1, 3, 2, 2, 5), True, True),      # messages: one faces_share of its own
+    ((1, 1, 1, 17, 3, 2, 8), False, False),
+]
+
+
+def make_fields(F, mix, seed0=11):
+    out = []
+    for i, (shape, periodic, messages) in enumerate(mix):
+        f = F.Faces(*shape, periodic=periodic, messages=messages)
+        u = f.field()
+        f.init_int(u, seed0 + i)
+        out.append((f, u))
+    return out
+
+
+def alone(F, mix, nshares, compute=True, seed0=11):
+    res = []
+    for f, u in make_fields(F, mix, seed0):
+        f.share_n(u, nshares, compute)
+        torch.cuda.synchronize()
+        res.append(u.cpu().numpy())
+        f.close()
+    return res
+
+
+def batched(F, mix, nshares, how, compute=True, seed0=11, tune=None):
+    fields = make_fields(F, mix, seed0)
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    if tune:
+        b.tune(*tune)
+    if how == "share":
+        for _ in range(nshares):
+            b.share(compute)
+    elif how == "graph":
+        b.share_n(nshares, compute)
+    else:
+        for _ in range(nshares):
+            b.share_each(compute)
+    torch.cuda.synchronize()
+    info = b.info()
+    b.close()
+    res = [u.cpu().numpy() for _, u in fields]
+    for f, _ in fields:
+        f.close()
+    return res, info
+
+
+@pytest.mark.parametrize("how", ["share", "graph", "each"])
+@pytest.mark.parametrize("compute", [True, False], ids=["compute", "nocompute"])
+def test_batch_equals_alone(faces_lib, how, compute):
+    F = faces_lib
+    ref = alone(F, MIX, 3, compute)
+    got, info = batched(F, MIX, 3, how, compute)
+    assert info["fields"] == len(MIX)
+    assert info["fused_fields"] == len(MIX) - 2
+    for i, (a, b) in enumerate(zip(ref, got)):
+        assert np.array_equal(a, b), f"field {i} {MIX[i]}"
+
+
+@pytest.mark.parametrize("tune", [(1, 1), (2, 2), (4, 3), (8, 0), (64, 1)], ids=str)
+def test_batch_work_split(faces_lib, tune):
+    F = faces_lib
+    ref = alone(F, MIX, 2)
+    got, info = batched(F, MIX, 2, "share", tune=tune)
+    assert info["unit_div"] == tune[0]
+    for i, (a, b) in enumerate(zip(ref, got)):
+        assert np.array_equal(a, b), f"field {i} {MIX[i]}"
+
+
+def test_batch_matches_oracle(oracle, faces_lib):
+    O, F = oracle, faces_lib
+    mix = MIX[:6]
+    got, _ = batched(F, mix, 2, "graph", seed0=3)
+    for i, ((shape, periodic, messages), out) in enumerate(zip(mix, got)):
+        s = O.Shape(*shape, periodic=periodic)
+        u = O.init_int(s, 3 + i)
+        for _ in range(2):
+            O.groups_share(s, u)
+        assert np.array_equal(u, out), f"field {i} {shape}"
+
+
+def test_graph_replay_and_autotune(faces_lib):
+    """A captured graph replays on later calls; autotune keeps results exact."""
+    F = faces_lib
+    mix = [((1, 1, 1, 6, 5, 4, n), n % 2 == 0, False) for n in range(2, 11)]
+    fields = make_fields(F, mix, 40)
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    applied = b.autotune(trials=1)
+    assert applied >= 8
+    for _ in range(3):
+        b.share_n(2)
+    torch.cuda.synchronize()
+    got = [u.cpu().numpy() for _, u in fields]
+    info = b.info()
+    b.close()
+    for f, _ in fields:
+        f.close()
+    ref = alone(F, mix, 6 + applied, seed0=40)
+    for i, (a, c) in enumerate(zip(ref, got)):
+        assert np.array_equal(a, c), f"field {i} {mix[i]} {info}"
+
+
+def test_many_fields(faces_lib):
+    """512 small fields of uneven shape in one launch."""
+    F = faces_lib
+    rng = np.random.default_rng(7)
+    mix = []
+    for _ in range(512):
+        n = int(rng.integers(2, 11))
+        m = tuple(int(x) for x in rng.integers(1, 5, size=3))
+        mix.append(((1, 1, 1) + m + (n,), bool(rng.integers(0, 2)), False))
+    ref = alone(F, mix, 2, seed0=100)
+    got, info = batched(F, mix, 2, "graph", seed0=100)
+    assert info["fused_fields"] == 512
+    bad = [i for i, (a, b) in enumerate(zip(ref, got)) if not np.array_equal(a, b)]
+    assert not bad, [mix[i] for i in bad[:5]]
