@@ -78,6 +78,23 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
     L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
+    jp, sp = ctypes.POINTER(FacesJob), ctypes.POINTER(ServeStats)
+    llp, dblp = ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)
+    L.faces_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_size_t, c_int, c_uint]
+    L.faces_server_submit.argtypes = [vp, jp, llp]
+    L.faces_server_poll.argtypes = [vp, c_int]
+    L.faces_server_drain.argtypes = [vp]
+    L.faces_server_job_status.argtypes = [vp, ctypes.c_longlong, ip, ip, dblp, dblp]
+    L.faces_server_field.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(vp), ctypes.POINTER(c_long)]
+    L.faces_server_fetch.argtypes = [vp, ctypes.c_longlong, dp]
+    L.faces_server_release.argtypes = [vp, ctypes.c_longlong]
+    L.faces_server_stats.argtypes = [vp, sp]
+    L.faces_server_run_trace.argtypes = [vp, c_int, jp, dblp, llp, dblp, dblp]
+    L.faces_server_destroy.argtypes = [vp]
+    for name in ("faces_server_create", "faces_server_submit", "faces_server_poll", "faces_server_drain",
+                 "faces_server_job_status", "faces_server_field", "faces_server_fetch", "faces_server_release",
+                 "faces_server_stats", "faces_server_run_trace", "faces_server_destroy"):
+        getattr(L, name).restype = c_int
     for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
                  "faces_share", "faces_share_n", "faces_init_ref", "faces_init_int", "faces_check",
                  "faces_run_host", "faces_set_tuning", "faces_launches_per_share", "faces_batch_create",
@@ -87,6 +104,37 @@ def lib() -> ctypes.CDLL:
         getattr(L, name).restype = c_int
     _lib = L
     return L
+
+
+class FacesJob(ctypes.Structure):
+    """struct faces_job of include/faces_gb300.h."""
+    _fields_ = [("lx", ctypes.c_int), ("ly", ctypes.c_int), ("lz", ctypes.c_int), ("mx", ctypes.c_int),
+                ("my", ctypes.c_int), ("mz", ctypes.c_int), ("n", ctypes.c_int), ("flags", ctypes.c_uint),
+                ("nshares", ctypes.c_int), ("init", ctypes.c_int), ("seed", ctypes.c_ulonglong),
+                ("host_in", ctypes.c_void_p)]
+
+
+class ServeStats(ctypes.Structure):
+    """struct faces_serve_stats of include/faces_gb300.h."""
+    _fields_ = [("submitted", ctypes.c_longlong), ("admitted", ctypes.c_longlong),
+                ("completed", ctypes.c_longlong), ("ticks", ctypes.c_longlong), ("launches", ctypes.c_longlong),
+                ("job_shares", ctypes.c_longlong), ("point_shares", ctypes.c_double),
+                ("resident_bytes", ctypes.c_size_t), ("peak_resident_bytes", ctypes.c_size_t),
+                ("budget_bytes", ctypes.c_size_t), ("queued", ctypes.c_int), ("running", ctypes.c_int)]
+
+
+def job(lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *, nshares: int, periodic: bool = False,
+        init: str = "int", seed: int = 0, host_in=None) -> FacesJob:
+    """A job for Server: a field of this shape, nshares shares.  init: "ref"
+    (gpu/main.cc:10-19), "int" (integer values from seed) or "host" (host_in,
+    a float64 numpy array of the field size, read when the job is admitted)."""
+    j = FacesJob(lx, ly, lz, mx, my, mz, n, PERIODIC if periodic else 0, nshares,
+                 {"ref": 0, "int": 1, "host": 2}[init], seed, None)
+    j._keep = None
+    if init == "host":
+        j.host_in = host_in.ctypes.data
+        j._keep = host_in
+    return j
 
 
 def _check(rc: int) -> int:
@@ -298,6 +346,103 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().faces_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+SERVE_PLAIN = 0x1
+SERVE_RELEASE_DONE = 0x2
+JOB_STATES = ("queued", "running", "done", "released")
+
+
+class Server:
+    """Halo-sum jobs arriving over time on one GPU (no counterpart in the
+    reference, which runs one job per process: gpu/main.cc:134-197).
+
+    Jobs are admitted in arrival order against an HBM budget (bytes) and run
+    together: every tick is one share of every running job in one persistent
+    launch.  plain=True launches the single-field kernel once per job per
+    tick instead (the one-field-per-launch form).  release_done frees a
+    job's field as soon as it is done (its result can then not be fetched).
+    """
+
+    def __init__(self, budget_bytes: int, max_jobs: int = 0, *, plain: bool = False, release_done: bool = False):
+        h = ctypes.c_void_p()
+        flags = (SERVE_PLAIN if plain else 0) | (SERVE_RELEASE_DONE if release_done else 0)
+        _check(lib().faces_server_create(ctypes.byref(h), int(budget_bytes), max_jobs, flags))
+        self._h = h
+        self._inputs = {}
+
+    def submit(self, j: FacesJob) -> int:
+        jid = ctypes.c_longlong()
+        _check(lib().faces_server_submit(self._h, ctypes.byref(j), ctypes.byref(jid)))
+        if getattr(j, "_keep", None) is not None:
+            self._inputs[jid.value] = j._keep  # read at admission
+        return jid.value
+
+    def poll(self, wait: bool = False) -> int:
+        return _check(lib().faces_server_poll(self._h, int(wait)))
+
+    def drain(self) -> int:
+        return _check(lib().faces_server_drain(self._h))
+
+    def status(self, jid: int) -> dict:
+        st, sd = ctypes.c_int(), ctypes.c_int()
+        w, lat = ctypes.c_double(), ctypes.c_double()
+        _check(lib().faces_server_job_status(self._h, jid, ctypes.byref(st), ctypes.byref(sd), ctypes.byref(w),
+                                             ctypes.byref(lat)))
+        return {"state": JOB_STATES[st.value], "shares_done": sd.value, "wait_s": w.value, "latency_s": lat.value}
+
+    def field_ptr(self, jid: int) -> tuple[int, int]:
+        p, tot = ctypes.c_void_p(), ctypes.c_long()
+        _check(lib().faces_server_field(self._h, jid, ctypes.byref(p), ctypes.byref(tot)))
+        return p.value, tot.value
+
+    def fetch(self, jid: int):
+        import numpy as np
+        _, tot = self.field_ptr(jid)
+        out = np.empty(tot, dtype=np.float64)
+        _check(lib().faces_server_fetch(self._h, jid, out.ctypes.data))
+        return out
+
+    def release(self, jid: int) -> None:
+        _check(lib().faces_server_release(self._h, jid))
+        self._inputs.pop(jid, None)
+
+    def stats(self) -> dict:
+        st = ServeStats()
+        _check(lib().faces_server_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServeStats._fields_}
+
+    def run_trace(self, jobs, arrivals):
+        """Replays arrivals (seconds, non-decreasing) in real time; returns
+        (job ids, latencies in seconds, makespan in seconds)."""
+        import numpy as np
+        nj = len(jobs)
+        arr = (FacesJob * nj)(*jobs)
+        t = np.ascontiguousarray(arrivals, dtype=np.float64)
+        ids = (ctypes.c_longlong * nj)()
+        lat = np.empty(nj, dtype=np.float64)
+        mk = ctypes.c_double()
+        _check(lib().faces_server_run_trace(self._h, nj, arr, t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            ids, lat.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            ctypes.byref(mk)))
+        return list(ids), lat, mk.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().faces_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

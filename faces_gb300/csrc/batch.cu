@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/faces_gb300.h"
+#include "batch_kernel.h"
 #include "ctx.h"
 #include "geom.cuh"
 #include "kernels.cuh"
@@ -39,7 +40,7 @@ namespace {
 __host__ __device__ constexpr int bk(int n) { return tile_kmax(n); }
 __host__ __device__ constexpr int bspt(int n) { return (n * n * pieces_per_row(n) + 255) / 256; }
 
-constexpr int kBatchMinN = 2, kBatchMaxN = 10, kBatchStages = 3;
+constexpr int kBatchStages = 3;
 constexpr int kNNMax = kBatchMaxN * kBatchMaxN;
 
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
@@ -52,15 +53,6 @@ __host__ __device__ constexpr int spt_max(int n) { return n < kBatchMinN ? 0 : c
 
 constexpr int kStage = (stage_max(kBatchMaxN) + 1) & ~1;
 constexpr int kSptMax = spt_max(kBatchMaxN);
-
-struct BatchField {
-  FieldDesc f;
-  RowPlan p;
-};
-
-struct BatchUnit {
-  int field, column, c0, c1;
-};
 
 // shared memory: data stages, then per-stage row arrays sized for n = 10
 constexpr long batch_smem_bytes()
@@ -228,6 +220,40 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
   }
 }
 
+}  // namespace
+
+RowPlan batch_plan(const FieldDesc &f)
+{
+  RowPlan p = make_row_plan(f, batch_n_supported(f.n) ? bk(f.n) : 1, 0);
+  p.order = 2;
+  p.unit_chunks = 1;
+  return p;
+}
+
+int batch_blocks_per_sm() { return std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024)))); }
+
+cudaError_t batch_configure()
+{
+  return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem_bytes());
+}
+
+void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, int unit_div)
+{
+  const long ncol = p.ntiles / p.nchunks;
+  const int uc = std::max(1, (p.nchunks + unit_div - 1) / unit_div);
+  for (int c0 = 0; c0 < p.nchunks; c0 += uc)
+    for (long col = 0; col < ncol; col++) units.push_back({field, (int)col, c0, std::min(c0 + uc, p.nchunks)});
+}
+
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, cudaStream_t s)
+{
+  if (nunits <= 0 || grid <= 0) return cudaSuccess;
+  batch_kernel<<<(unsigned)grid, 256, batch_smem_bytes(), s>>>(d_fields, d_units, nunits);
+  return cudaGetLastError();
+}
+
+namespace {
+
 int fail(int code, const char *fmt, ...)
 {
   char buf[512];
@@ -273,7 +299,7 @@ namespace {
 
 bool batch_eligible(const faces_ctx *c)
 {
-  return c->n >= kBatchMinN && c->n <= kBatchMaxN && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS));
+  return batch_n_supported(c->n) && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS));
 }
 
 void drop_graphs(faces_batch *b)
@@ -292,13 +318,7 @@ int build_units(faces_batch *b)
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t a, size_t c) { return b->h_fields[a].f.n < b->h_fields[c].f.n; });
   std::vector<BatchUnit> units;
-  for (size_t i : order) {
-    const RowPlan &p = b->h_fields[i].p;
-    const long ncol = p.ntiles / p.nchunks;
-    const int uc = std::max(1, (p.nchunks + b->unit_div - 1) / b->unit_div);
-    for (int c0 = 0; c0 < p.nchunks; c0 += uc)
-      for (long col = 0; col < ncol; col++) units.push_back({(int)i, (int)col, c0, std::min(c0 + uc, p.nchunks)});
-  }
+  for (size_t i : order) append_units(units, (int)i, b->h_fields[i].p, b->unit_div);
   cudaFree(b->d_units);
   b->d_units = nullptr;
   b->nunits = (int)units.size();
@@ -314,9 +334,7 @@ int build_units(faces_batch *b)
 
 int launch_batched(faces_batch *b, cudaStream_t s)
 {
-  if (b->nunits == 0) return FACES_OK;
-  batch_kernel<<<(unsigned)b->grid, 256, batch_smem_bytes(), s>>>(b->d_fields, b->d_units, b->nunits);
-  CUDA_TRY(cudaGetLastError(), "batch kernel launch");
+  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, s), "batch kernel launch");
   return FACES_OK;
 }
 
@@ -380,9 +398,7 @@ int faces_batch_commit(faces_batch *b)
     const faces_ctx *c = b->ctx[i];
     BatchField bf;
     bf.f = c->desc(b->u[i]);
-    bf.p = make_row_plan(bf.f, c->n >= kBatchMinN && c->n <= kBatchMaxN ? bk(c->n) : 1, 0);
-    bf.p.order = 2;
-    bf.p.unit_chunks = 1;
+    bf.p = batch_plan(bf.f);
     b->h_fields[i] = bf;
     b->fused[i] = batch_eligible(c) ? 1 : 0;
   }
@@ -391,9 +407,8 @@ int faces_batch_commit(faces_batch *b)
     CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * nf, cudaMemcpyHostToDevice),
              "faces_batch: field table upload");
   }
-  CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem_bytes()),
-           "faces_batch: shared memory attribute");
-  b->per_sm = std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  CUDA_TRY(batch_configure(), "faces_batch: shared memory attribute");
+  b->per_sm = batch_blocks_per_sm();
   CUDA_TRY(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "faces_batch: capture stream");
   b->committed = true;
   return build_units(b);
@@ -448,7 +463,7 @@ int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm)
 {
   if (int rc = check_batch(b, true)) return rc;
   if (unit_div > 0) b->unit_div = unit_div;
-  if (blocks_per_sm > 0) b->per_sm = std::min(blocks_per_sm, std::max(1, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  if (blocks_per_sm > 0) b->per_sm = std::min(blocks_per_sm, batch_blocks_per_sm());
   return build_units(b);
 }
 
@@ -457,7 +472,7 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
   if (int rc = check_batch(b, true)) return rc;
   if (trials < 1) trials = 3;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int fit = std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024))));
+  const int fit = batch_blocks_per_sm();
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
   CUDA_TRY(cudaEventCreate(&e1), "autotune: event");

@@ -1,0 +1,47 @@
+// batch_kernel.h -- the batched tile kernel as used by batches (batch.cu) and
+// the job server (serve.cu): a device table of fields and a device work list
+// of column units, one persistent launch per share of every listed field.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "geom.cuh"
+#include "rows_setup.cuh"
+
+namespace faces {
+
+constexpr int kBatchMinN = 2, kBatchMaxN = 10;
+
+struct BatchField {
+  FieldDesc f;
+  RowPlan p;  // from batch_plan
+};
+
+// x-chunks [c0, c1) of one element column of field `field`
+struct BatchUnit {
+  int field, column, c0, c1;
+};
+
+// n the batched kernel handles (direct mode only)
+inline bool batch_n_supported(int n) { return n >= kBatchMinN && n <= kBatchMaxN; }
+
+// the tile plan of a field in the batched kernel
+RowPlan batch_plan(const FieldDesc &f);
+
+// resident blocks per SM the kernel's shared memory allows (at most 3)
+int batch_blocks_per_sm();
+
+// sets the kernel's shared-memory attribute on the current device (call once
+// per device before the first launch)
+cudaError_t batch_configure();
+
+// appends the units of field `field` (column units cut into unit_div parts)
+void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, int unit_div);
+
+// one share of every field the units cover; grid blocks stride over the units
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid,
+                         cudaStream_t s);
+
+}  // namespace faces

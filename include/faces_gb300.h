@@ -191,6 +191,89 @@ int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *
 
 int faces_batch_destroy(faces_batch *b);
 
+/* ---- Job server: halo-sum jobs arriving over time ----
+ *
+ * The reference runs one job per launch of its executable (gpu/main.cc:134-
+ * 197: one field, nk*nj*ni shares, then exit).  A server keeps many jobs of
+ * different sizes resident on one GPU: each job is admitted, in arrival
+ * order, when its field fits the HBM budget (and the job limit); from then
+ * on every running job takes one share per tick, all of them in one
+ * persistent launch (continuous batching: jobs that arrive while others run
+ * join at the next tick, finished ones leave).  A job's result is bit for
+ * bit the field faces_share_n gives it alone.  Jobs run in direct mode with
+ * 2 <= n <= 10.  One host thread at a time may call a server. */
+typedef struct faces_server faces_server;
+
+typedef struct faces_job {
+  int lx, ly, lz, mx, my, mz, n; /* as faces_create */
+  unsigned flags;                /* FACES_PERIODIC or 0 */
+  int nshares;                   /* shares to run (nk*nj*ni), >= 1 */
+  int init;                      /* 0: faces_init_ref, 1: faces_init_int(seed), 2: copy host_in */
+  unsigned long long seed;
+  const double *host_in;         /* init = 2: the field (total doubles), read during admission */
+} faces_job;
+
+typedef struct faces_serve_stats {
+  long long submitted, admitted, completed;
+  long long ticks;      /* scheduling rounds, each one share of every running job */
+  long long launches;   /* kernel launches (steps and initialisations) */
+  long long job_shares; /* shares run, summed over jobs */
+  double point_shares;  /* points times shares, summed over jobs */
+  size_t resident_bytes, peak_resident_bytes, budget_bytes;
+  int queued, running;
+} faces_serve_stats;
+
+#define FACES_SERVE_PLAIN 0x1u        /* one single-field launch per running job per tick (the plain form) */
+#define FACES_SERVE_RELEASE_DONE 0x2u /* free a job's field as soon as it is done */
+
+/* A server with an HBM budget for job fields (bytes) and a limit on running
+ * jobs (<= 0: none).  Its memory comes from a stream-ordered pool that keeps
+ * what it has taken until faces_server_destroy. */
+int faces_server_create(faces_server **s, size_t budget_bytes, int max_jobs, unsigned flags);
+
+/* Queues a job (arrival = now); rejected if its field alone exceeds the
+ * budget.  *job_id identifies it afterwards. */
+int faces_server_submit(faces_server *s, const faces_job *job, long long *job_id);
+
+/* One scheduling round: retire finished ticks, admit, launch the next tick.
+ * wait != 0: when no launch is possible, block until the oldest tick
+ * finishes.  Returns the jobs that became done (>= 0) or an error code;
+ * FACES_ENOMEM when a queued job can never be admitted because done jobs
+ * that were not released hold the budget. */
+int faces_server_poll(faces_server *s, int wait);
+
+/* Polls until every submitted job is done; returns the jobs that became done. */
+int faces_server_drain(faces_server *s);
+
+/* state: 0 queued, 1 running, 2 done, 3 released; shares done; seconds from
+ * arrival to admission (wait_s) and to the GPU completion of its last share
+ * (latency_s), -1 while not reached.  Any pointer may be NULL. */
+int faces_server_job_status(faces_server *s, long long job_id, int *state, int *shares_done, double *wait_s,
+                            double *latency_s);
+
+/* Device field of a running or done job and its size in doubles. */
+int faces_server_field(faces_server *s, long long job_id, double **u, long *total_doubles);
+
+/* Copies a done job's field to host memory (synchronous). */
+int faces_server_fetch(faces_server *s, long long job_id, double *host_out);
+
+/* Frees a done job's field and forgets the job. */
+int faces_server_release(faces_server *s, long long job_id);
+
+int faces_server_stats(const faces_server *s, faces_serve_stats *st);
+
+/* Replays an arrival trace in real time: job i is submitted when
+ * arrival_s[i] seconds (non-decreasing) have passed since the call began,
+ * stamped with that time, and the call returns when all are done.
+ * job_ids[i], latency_s[i] (arrival to completion) and *makespan_s may be
+ * NULL. */
+int faces_server_run_trace(faces_server *s, int njobs, const faces_job *jobs, const double *arrival_s,
+                           long long *job_ids, double *latency_s, double *makespan_s);
+
+/* Waits for the server's work and frees everything it holds.  NULL is
+ * accepted. */
+int faces_server_destroy(faces_server *s);
+
 #ifdef __cplusplus
 }
 #endif

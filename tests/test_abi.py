@@ -60,3 +60,21 @@ def test_executable_prints_reference_header_lines(faces_lib):
                          "1 face inits x 2 element inits x 5 shares without compute kernels"]
     r = subprocess.run([exe], input="1 2\n", capture_output=True, text=True, timeout=60)
     assert r.returncode == 2
+
+
+def test_struct_layouts_match_header(faces_lib, tmp_path):
+    """The ctypes mirrors of faces_job and faces_serve_stats have the C layout."""
+    F = faces_lib
+    src = tmp_path / "layout.c"
+    src.write_text(
+        "#include <stdio.h>\n#include <stddef.h>\n#include \"faces_gb300.h\"\n"
+        "int main(void) {\n"
+        "  printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(faces_job), offsetof(faces_job, seed),\n"
+        "         offsetof(faces_job, host_in), sizeof(faces_serve_stats),\n"
+        "         offsetof(faces_serve_stats, point_shares), offsetof(faces_serve_stats, queued));\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [ctypes.sizeof(F.FacesJob), F.FacesJob.seed.offset, F.FacesJob.host_in.offset,
+                   ctypes.sizeof(F.ServeStats), F.ServeStats.point_shares.offset, F.ServeStats.queued.offset]
