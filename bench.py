@@ -21,6 +21,11 @@ cpu_baseline = the reference's v-26 pack/inner/unpack loops transcribed to
 --impl reference times that CPU implementation alone (the reference's own
 Mugs/Faces code cannot run on this machine: see the design doc).
 
+batched  = 512 fields of mixed shape advanced by one persistent launch per
+            share, against one launch per field (steps/s of each)
+served   = a 400-job Poisson trace through the job server, batched and
+            plain: steps/s and p50/p99 latency (rank 0 only)
+
 With N > 1 (torchrun) every rank advances its own copy of the field on its
 GPU: independent fields, no collective on the data path (weak scaling).
 """
@@ -318,7 +323,147 @@ def run_faces(args) -> dict | None:
     }
     if world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline()
+    if not args.no_mixed:
+        del u
+        f.close()
+        torch.cuda.empty_cache()
+        out["batched"] = batched_leg(F, dev)
+        out["served"] = served_leg(F)
     return out
+
+
+# ---------------------------------------------------------------------------
+# batched and served workloads (reported beside the headline, rank 0 only)
+# ---------------------------------------------------------------------------
+
+C4_FIELDS, C4_STEPS = 512, 20
+C5_JOBS, C5_BUDGET = 400, 150 << 30
+
+
+def c4_mix(seed: int = 4, nfields: int = C4_FIELDS) -> list[tuple]:
+    """512 periodic single-rank fields, mx,my,mz uniform in [2,24], n uniform in {3..10}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    mix = []
+    for _ in range(nfields):
+        m = tuple(int(x) for x in rng.integers(2, 25, size=3))
+        mix.append((1, 1, 1) + m + (int(rng.integers(3, 11)),))
+    return mix
+
+
+def c5_jobs(F, count: int = C5_JOBS, seed: int = 5) -> list:
+    """Jobs of rank grid {1,2}^3, m per dimension log-uniform in [2,32], n uniform
+    in {4..8}, 10..200 shares, periodic, integer-valued fields seeded per job."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(count):
+        L = [int(x) for x in rng.integers(1, 3, size=3)]
+        m = [int(np.floor(np.exp(rng.uniform(np.log(2), np.log(33))))) for _ in range(3)]
+        n = int(rng.integers(4, 9))
+        jobs.append(F.job(*L, *m, n, nshares=int(rng.integers(10, 201)), periodic=True, init="int", seed=i))
+    return jobs
+
+
+def _events_ms(fn, stream, reps: int) -> float:
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def batched_leg(F, dev) -> dict:
+    """C4: one persistent launch per share of all 512 fields (a CUDA graph of
+    20 shares), against one launch of the single-field kernel per field."""
+    import torch
+    mix = c4_mix()
+    fields = []
+    for i, sh in enumerate(mix):
+        f = F.Faces(*sh, periodic=True)
+        fields.append((f, f.field(dev)))
+    points = sum(f.points for f, _ in fields)
+    stream = torch.cuda.current_stream(dev)
+
+    def reinit():
+        for i, (f, u) in enumerate(fields):
+            f.init_int(u, 100 + i, stream)
+
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    reinit()
+    b.autotune(3, stream)
+    info = b.info()
+    reinit()
+    b.share_n(C4_STEPS, True, stream)  # warm-up (captures the graph)
+    reinit()
+    ms_batched = _events_ms(lambda: b.share_n(C4_STEPS, True, stream), stream, 1) / C4_STEPS
+    sample = list(range(0, len(fields), 37))
+    checks = [fields[i][0].check(fields[i][1], init="int", seed=100 + i, nshares=C4_STEPS) for i in sample]
+    reinit()
+    b.share_each(True, stream)  # warm-up
+    reinit()
+    ms_plain = _events_ms(lambda: b.share_each(True, stream), stream, C4_STEPS)
+    b.close()
+    for f, _ in fields:
+        f.close()
+    del fields
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"{len(mix)} periodic single-rank fields, mx,my,mz uniform in [2,24], n uniform in {{3..10}} "
+                    f"({points:,} points, seeded per field), {C4_STEPS} shares",
+        "steps_per_s": round(1e3 / ms_batched, 2),
+        "plain_steps_per_s": round(1e3 / ms_plain, 2),
+        "speedup_vs_plain": round(ms_plain / ms_batched, 3),
+        "gbs": round(16 * points / (ms_batched * 1e-3) / 1e9, 1),
+        "plain_gbs": round(16 * points / (ms_plain * 1e-3) / 1e9, 1),
+        "launches_per_step": 1, "plain_launches_per_step": len(mix),
+        "autotuned": info,
+        "batched": "CUDA graph of 20 launches of the batched tile kernel (faces_batch_share_n)",
+        "plain": "one faces_share per field per share (faces_batch_share_each)",
+        "check": {"fields_checked": len(sample), "max_maxrel": max(c.maxrel for c in checks),
+                  "passed": all(c.passed for c in checks)},
+    }
+
+
+def served_leg(F) -> dict:
+    """C5: a 400-job Poisson trace through the job server, batched and plain."""
+    import numpy as np
+    jobs = c5_jobs(F)
+    shares = sum(j.nshares for j in jobs)
+    pts = sum(j.lx * j.ly * j.lz * j.mx * j.my * j.mz * j.n ** 3 * j.nshares for j in jobs)
+    runs = []
+    for plain, rates in ((False, (float("inf"), 1000.0, 500.0)), (True, (float("inf"), 1000.0))):
+        for rate in rates:
+            rng = np.random.default_rng(7)
+            arr = (np.zeros(len(jobs)) if rate == float("inf")
+                   else np.cumsum(rng.exponential(1.0 / rate, size=len(jobs))))
+            with F.Server(C5_BUDGET, plain=plain, release_done=True) as srv:
+                srv.run_trace(jobs[:8], np.zeros(8))  # warm-up
+                _, lat, mk = srv.run_trace(jobs, arr)
+                st = srv.stats()
+            runs.append({"form": "plain" if plain else "batched",
+                         "rate_jobs_per_s": None if rate == float("inf") else rate,
+                         "steps_per_s": round(shares / mk, 1), "gbs": round(16 * pts / mk / 1e9, 1),
+                         "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                         "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+                         "makespan_s": round(mk, 4), "ticks": st["ticks"], "launches": st["launches"],
+                         "peak_resident_gb": round(st["peak_resident_bytes"] / 1e9, 3)})
+    sat = {r["form"]: r["steps_per_s"] for r in runs if r["rate_jobs_per_s"] is None}
+    return {
+        "workload": f"{len(jobs)} jobs: rank grid in {{1,2}}^3, m per dimension log-uniform in [2,32], n uniform in "
+                    "{4..8}, 10..200 shares, periodic, integer fields; Poisson arrivals (rate inf = all at t=0)",
+        "budget_gb": C5_BUDGET / 2 ** 30,
+        "steps": "job shares (one share of one job)",
+        "runs": runs,
+        "speedup_vs_plain_saturated": round(sat["batched"] / sat["plain"], 3),
+        "latency": "arrival to GPU completion of the job's last share",
+    }
 
 
 def run_reference(args) -> dict | None:
@@ -352,6 +497,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["faces", "reference"], default="faces")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the batched and served legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     out = run_reference(args) if args.impl == "reference" else run_faces(args)
