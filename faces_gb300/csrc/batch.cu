@@ -27,6 +27,7 @@
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
 #include "tile_steps.cuh"
+#include "ptile_steps.cuh"
 
 void faces_internal_set_error(const char *msg);
 
@@ -59,7 +60,7 @@ constexpr long batch_smem_bytes()
 {
   return sizeof(double) * (long)kBatchStages * kStage + sizeof(double *) * (long)kBatchStages * kNNMax +
          sizeof(SlotCol) * (long)kBatchStages * kNNMax + sizeof(unsigned) * (long)kBatchStages * kNNMax +
-         sizeof(int4) * kBatchStages;
+         sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages;
 }
 
 struct BWalk {
@@ -99,6 +100,7 @@ struct Smem {
   SlotCol *rinfo;
   unsigned *rfl;
   int4 *tinfo;
+  PMeta *meta;
 };
 
 __device__ __forceinline__ Smem smem_layout(double *sm)
@@ -111,26 +113,33 @@ __device__ __forceinline__ Smem smem_layout(double *sm)
   m.rinfo = reinterpret_cast<SlotCol *>(m.lop + kBatchStages * kNNMax);
   m.rfl = reinterpret_cast<unsigned *>(m.rinfo + kBatchStages * kNNMax);
   m.tinfo = reinterpret_cast<int4 *>(m.rfl + kBatchStages * kNNMax);
+  m.meta = reinterpret_cast<PMeta *>(m.tinfo + kBatchStages);
   return m;
 }
 
-template <int N>
+// MODE: 0 every field takes the general step, 1 every field the periodic
+// step, 2 each field its own
+template <int N, int MODE>
 __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u, ColKey &ck, bool &have_col,
                                        SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
-  stage_tile<N, bk(N), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage, m.rfl + st * kNNMax,
-                            m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
+  if (MODE == 1 || (MODE == 2 && bf.lean))
+    ptile::pstage<N, bk(N)>(bf.f, bf.p, u, m.data + (long)st * kStage, m.meta + st, m.tinfo + st);
+  else
+    stage_tile<N, bk(N), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage,
+                                  m.rfl + st * kNNMax, m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
 }
 
 // stage tile u of field `field` into stage st; the tile info's z holds
-// hi_x | n << 1 and w the field
+// hi_x | lean << 1 | n << 2 and w the field
+template <int MODE>
 __device__ __forceinline__ void bstage_any(const BatchField *fields, int field, const TileCursor &u, ColKey &ck,
                                            bool &have_col, SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
   const BatchField &bf = fields[field];
   switch (bf.f.n) {
 #define FACES_BSTAGE(NV) \
-  case NV: bstage<NV>(bf, u, ck, have_col, col, m, st); break;
+  case NV: bstage<NV, MODE>(bf, u, ck, have_col, col, m, st); break;
     FACES_BSTAGE(2) FACES_BSTAGE(3) FACES_BSTAGE(4) FACES_BSTAGE(5) FACES_BSTAGE(6) FACES_BSTAGE(7) FACES_BSTAGE(8)
     FACES_BSTAGE(9) FACES_BSTAGE(10)
 #undef FACES_BSTAGE
@@ -141,12 +150,13 @@ __device__ __forceinline__ void bstage_any(const BatchField *fields, int field, 
   }
   if (threadIdx.x == 0) {
     int4 ti = m.tinfo[st];
-    ti.z = (ti.z & 1) | (bf.f.n << 1);
+    ti.z = (ti.z & 1) | ((MODE == 1 || (MODE == 2 && bf.lean)) ? 2 : 0) | (bf.f.n << 2);
     ti.w = field;
     m.tinfo[st] = ti;
   }
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits)
 {
   extern __shared__ __align__(16) double sm[];
@@ -165,7 +175,7 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
   for (int j = 0; j < kBatchStages - 1; j++) {
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any(fields, nw.field, nw.cur, ck, have_col, col, m, j);
+      bstage_any<MODE>(fields, nw.field, nw.cur, ck, have_col, col, m, j);
       bwalk_next(fields, units, nunits, nw);
       inflight++;
     } else {
@@ -178,15 +188,15 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
     cp_wait<kBatchStages - 2>();
     const unsigned *rfl = m.rfl + s * kNNMax;
     const int4 ti = m.tinfo[s];
-    const int nk = ti.y, n = ti.z >> 1;
-    const bool hx = (ti.z & 1) != 0;
+    const int nk = ti.y, n = ti.z >> 2;
+    const bool hx = (ti.z & 1) != 0, lean = MODE == 1 || (MODE == 2 && (ti.z & 2) != 0);
     bool ok = true;
-    if ((int)threadIdx.x < n * n) ok = row_regular(rfl[threadIdx.x], hx);
+    if (!lean && (int)threadIdx.x < n * n) ok = row_regular(rfl[threadIdx.x], hx);
     const int regular = __syncthreads_and(ok);
     const int sn = (s + kBatchStages - 1) % kBatchStages;
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
+      bstage_any<MODE>(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
       bwalk_next(fields, units, nunits, nw);
       inflight++;
     } else {
@@ -206,9 +216,12 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
     __syncthreads();
     if (nk > 0) {
       switch (n) {
-#define FACES_BSTORE(NV)                                                                                \
-  case NV:                                                                                               \
-    store_tile<NV, bk(NV), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
+#define FACES_BSTORE(NV)                                                                                  \
+  case NV:                                                                                                 \
+    if (lean)                                                                                              \
+      ptile::pstore<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk);                                      \
+    else                                                                                                   \
+      store_tile<NV, bk(NV), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;
         FACES_BSTORE(2) FACES_BSTORE(3) FACES_BSTORE(4) FACES_BSTORE(5) FACES_BSTORE(6) FACES_BSTORE(7)
         FACES_BSTORE(8) FACES_BSTORE(9) FACES_BSTORE(10)
@@ -234,7 +247,18 @@ int batch_blocks_per_sm() { return std::max(1, std::min(3, (int)((228 * 1024) / 
 
 cudaError_t batch_configure()
 {
-  return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem_bytes());
+  const int smem = (int)batch_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(batch_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
+int batch_mode(const BatchField *fields, size_t n)
+{
+  size_t lean = 0;
+  for (size_t i = 0; i < n; i++) lean += fields[i].lean ? 1 : 0;
+  return lean == 0 ? 0 : lean == n ? 1 : 2;
 }
 
 void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, int unit_div)
@@ -245,10 +269,14 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
     for (long col = 0; col < ncol; col++) units.push_back({field, (int)col, c0, std::min(c0 + uc, p.nchunks)});
 }
 
-cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, cudaStream_t s)
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
+                         cudaStream_t s)
 {
   if (nunits <= 0 || grid <= 0) return cudaSuccess;
-  batch_kernel<<<(unsigned)grid, 256, batch_smem_bytes(), s>>>(d_fields, d_units, nunits);
+  const size_t smem = batch_smem_bytes();
+  if (mode == 1) batch_kernel<1><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  else if (mode == 2) batch_kernel<2><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  else batch_kernel<0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
   return cudaGetLastError();
 }
 
@@ -286,6 +314,7 @@ struct faces_batch {
   BatchField *d_fields = nullptr;
   BatchUnit *d_units = nullptr;
   int nunits = 0;
+  int mode = 0;      // batch_mode of the fused fields
   int unit_div = 2;  // units are 1/unit_div of a column's chunks
   int per_sm = 3;
   int sms = 0;
@@ -318,7 +347,12 @@ int build_units(faces_batch *b)
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t a, size_t c) { return b->h_fields[a].f.n < b->h_fields[c].f.n; });
   std::vector<BatchUnit> units;
-  for (size_t i : order) append_units(units, (int)i, b->h_fields[i].p, b->unit_div);
+  std::vector<BatchField> fused;
+  for (size_t i : order) {
+    append_units(units, (int)i, b->h_fields[i].p, b->unit_div);
+    fused.push_back(b->h_fields[i]);
+  }
+  b->mode = batch_mode(fused.data(), fused.size());
   cudaFree(b->d_units);
   b->d_units = nullptr;
   b->nunits = (int)units.size();
@@ -334,7 +368,7 @@ int build_units(faces_batch *b)
 
 int launch_batched(faces_batch *b, cudaStream_t s)
 {
-  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, s), "batch kernel launch");
+  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->mode, s), "batch kernel launch");
   return FACES_OK;
 }
 
@@ -399,6 +433,7 @@ int faces_batch_commit(faces_batch *b)
     BatchField bf;
     bf.f = c->desc(b->u[i]);
     bf.p = batch_plan(bf.f);
+    bf.lean = ptile_field(bf.f) && !(c->flags & FACES_GENERAL);
     b->h_fields[i] = bf;
     b->fused[i] = batch_eligible(c) ? 1 : 0;
   }

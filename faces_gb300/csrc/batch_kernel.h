@@ -17,6 +17,7 @@ constexpr int kBatchMinN = 2, kBatchMaxN = 10;
 struct BatchField {
   FieldDesc f;
   RowPlan p;  // from batch_plan
+  int lean;   // 1: the periodic tile step (ptile_steps.cuh), 0: the general one
 };
 
 // x-chunks [c0, c1) of one element column of field `field`
@@ -40,8 +41,11 @@ cudaError_t batch_configure();
 // appends the units of field `field` (column units cut into unit_div parts)
 void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, int unit_div);
 
+// the kernel form for a field table: 0 all general, 1 all periodic (lean), 2 mixed
+int batch_mode(const BatchField *fields, size_t n);
+
 // one share of every field the units cover; grid blocks stride over the units
-cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid,
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
                          cudaStream_t s);
 
 }  // namespace faces

@@ -127,7 +127,7 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   if (lx < 1 || ly < 1 || lz < 1) return fail(FACES_EINVAL, "rank grid %d x %d x %d must be positive", lx, ly, lz);
   if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
   if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
-  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS))
+  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL))
     return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
   const long nranks = (long)lx * ly * lz;
   if (nranks > 65535 / 27) return fail(FACES_EINVAL, "%ld ranks: at most %d virtual ranks", nranks, 65535 / 27);
@@ -239,7 +239,7 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   const bool fused = compute && !(c->flags & FACES_GATHER);
   if (fused && !(c->flags & FACES_ROWS) && tile_kernel_supported(c->n))
-    CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s), "tile kernel launch");
+    CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, (c->flags & FACES_GENERAL) != 0), "tile kernel launch");
   else if (fused && row_kernel_supported(c->n))
     CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
   else

@@ -20,7 +20,8 @@ cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);
 size_t tile_smem_bytes(int n, int chunk);
-cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);
+// periodic direct-mode fields take the periodic tile step unless `general`
+cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false);
 
 // Closed-form check of a field after `nshares` shares of a known initial
 // state (init: 0 = reference formula, 1 = integer seed) with the relative

@@ -1,0 +1,195 @@
+// ptile_steps.cuh -- the tile step for direct-mode periodic fields.
+//
+// In a periodic field every tile is regular: every staged row exists, every
+// row has its x-lower end, and no tile takes an x-upper end.  A row's
+// source then needs no per-row setup: slot (sy, sz) of a tile of column
+// (rank, jy, jz) is row (iy, iz) = (sy, sz) of the element in one of four
+// columns -- (jy, jz), (jy-1, jz), (jy, jz-1), (jy-1, jz-1), chosen by
+// sy == n-1 and sz == n-1, wrapping to the neighbour rank -- and its x-lower
+// end is point n-1 of element jx0-1, or of element mx-1 of the x-lower
+// neighbour rank for the first chunk.  Only the pieces the passes use are
+// moved: both ends of the interior rows, the seam rows in full.  The shared-memory
+// layout is the general tile step's, so the dense passes (sum_tile) are
+// shared.  What each tile reads and writes is exactly what the general step
+// reads and writes for a regular tile.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "geom.cuh"
+#include "rows_setup.cuh"
+#include "tile_ops.cuh"
+#include "tile_steps.cuh"
+
+namespace faces {
+
+// offsets (doubles from the field base) of a tile's four columns at its
+// first element and of their x-lower end elements; column s: bit 0 the
+// y-lower column, bit 1 the z-lower column
+struct PMeta {
+  long off[4];
+  long lo[4];
+};
+
+// a field whose tiles the periodic step takes
+FACES_HD bool ptile_field(const FieldDesc &f) { return f.periodic && f.mode == kDirect; }
+
+namespace ptile {
+
+using namespace tiledev;
+
+template <int N>
+__device__ __forceinline__ long col_off(const FieldDesc &f, const TileCursor &u, int s, bool xlower, int jx)
+{
+  const bool ly = (s & 1) != 0, lz = (s & 2) != 0;
+  const int dy = (ly && u.jy == 0) ? -1 : 0, dz = (lz && u.jz == 0) ? -1 : 0, dx = xlower ? -1 : 0;
+  const int jy = ly ? (u.jy == 0 ? f.m[1] - 1 : u.jy - 1) : u.jy;
+  const int jz = lz ? (u.jz == 0 ? f.m[2] - 1 : u.jz - 1) : u.jz;
+  int q = u.r;
+  if (f.nranks > 1 && (dx | dy | dz)) q = __ldg(f.nbr + u.r * 27 + dir_index(dx, dy, dz));
+  return (long)q * f.R + (long)jz * f.sjz + (long)jy * f.sjy + (long)jx * (N * N * N);
+}
+
+// the column of slot r
+template <int N>
+__device__ __forceinline__ int col_sel(int sy, int sz)
+{
+  return (sy == N - 1 ? 1 : 0) | (sz == N - 1 ? 2 : 0);
+}
+
+// The pieces a tile moves per element: the two end pieces of each interior
+// row (1 <= sy, sz <= n-2), then every piece of each seam row.  Item j of an
+// element -> row (sy, sz) and piece pc.
+template <int N>
+struct Needed {
+  static constexpr int NP = pieces_per_row(N), NI = (N - 2) * (N - 2), NB = N * N - NI;
+  static constexpr int count = NI * (NP > 1 ? 2 : 1) + NB * NP;
+};
+
+template <int N>
+__device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, int &pc)
+{
+  constexpr int NP = Needed<N>::NP, NI = Needed<N>::NI, E = NP > 1 ? 2 : 1;
+  if constexpr (NI > 0) {
+    if (j < NI * E) {
+      const int ri = j / E;
+      pc = (j - ri * E) ? NP - 1 : 0;
+      sy = 1 + ri % (N - 2);
+      sz = 1 + ri / (N - 2);
+      return;
+    }
+  }
+  j -= NI * E;
+  const int b = j / NP;
+  pc = j - b * NP;
+  if (b < N) { sy = b; sz = 0; }
+  else if (b < 2 * N) { sy = b - N; sz = N - 1; }
+  else {
+    const int t = b - 2 * N;
+    sz = 1 + t / 2;
+    sy = (t & 1) ? N - 1 : 0;
+  }
+}
+
+// Threads and needed slots: with more than 128 slots per element thread t
+// takes slots t, t+256, ... (SPT of them) for every element of the tile;
+// with fewer, KT = 256/slots threads share a slot and thread t takes its
+// elements t/slots, +KT, ...  A thread decodes its slot once per tile and
+// walks the elements by adding the element stride.
+template <int N>
+struct PSlots {
+  static constexpr int NE = Needed<N>::count;
+  static constexpr int KT = NE <= 128 ? 256 / NE : 1;
+  static constexpr int SPT = KT > 1 ? 1 : (NE + 255) / 256;
+};
+
+template <int N>
+__device__ __forceinline__ bool pslot(int jj, int &j, int &kq)
+{
+  constexpr int NE = PSlots<N>::NE, KT = PSlots<N>::KT;
+  if constexpr (KT > 1) {
+    j = (int)threadIdx.x % NE;
+    kq = (int)threadIdx.x / NE;
+    return kq < KT;
+  } else {
+    j = (int)threadIdx.x + jj * 256;
+    kq = 0;
+    return j < NE;
+  }
+}
+
+// Stage tile u: the needed pieces of its elements, and the x-lower ends.
+template <int N, int K>
+__device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, const TileCursor &u, double *buf,
+                                       PMeta *meta, int4 *tinfo)
+{
+  constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int KT = PSlots<N>::KT, SPT = PSlots<N>::SPT;
+  constexpr long N3 = (long)N * N * N;
+  const int jx0 = u.c * p.chunk;
+  const int nk = min(p.chunk, f.m[0] - jx0);
+  const bool first = u.c == 0;
+  const int jxl = first ? f.m[0] - 1 : jx0 - 1;
+  if (threadIdx.x < 4) {
+    const int s = threadIdx.x;
+    meta->off[s] = col_off<N>(f, u, s, false, jx0);
+    meta->lo[s] = col_off<N>(f, u, s, first, jxl);
+  }
+  if (threadIdx.x == 0) *tinfo = make_int4(jx0, nk, 0, 0);
+  const long o0 = col_off<N>(f, u, 0, false, jx0), o1 = col_off<N>(f, u, 1, false, jx0);
+  const long o2 = col_off<N>(f, u, 2, false, jx0), o3 = col_off<N>(f, u, 3, false, jx0);
+#pragma unroll
+  for (int jj = 0; jj < SPT; jj++) {
+    int j, kq;
+    if (!pslot<N>(jj, j, kq)) continue;
+    int sy, sz, pc;
+    needed_piece<N>(j, sy, sz, pc);
+    const int s = col_sel<N>(sy, sz);
+    const long o = s == 0 ? o0 : s == 1 ? o1 : s == 2 ? o2 : o3;
+    const double *g = f.u + o + kq * N3 + sz * NN + sy * N + pc * PW;
+    double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
+    for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) cp_async(sp, g, PW);
+  }
+  if ((int)threadIdx.x < NN) {
+    const int r = threadIdx.x, sy = r % N, sz = r / N;
+    const long ol = col_off<N>(f, u, col_sel<N>(sy, sz), first, jxl);
+    cp_async(buf + K * NN * RS + r, f.u + ol + sz * NN + sy * N + (N - 1), 1);
+  }
+  cp_commit();
+}
+
+// Store the changed points: the staged pieces, all but the last element's
+// point n-1 (the next chunk's seam), and the x-lower ends.
+template <int N, int K>
+__device__ __forceinline__ void pstore(const FieldDesc &f, const double *buf, const PMeta *meta, int nk)
+{
+  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int KT = PSlots<N>::KT, SPT = PSlots<N>::SPT;
+  constexpr long N3 = (long)N * N * N;
+#pragma unroll
+  for (int jj = 0; jj < SPT; jj++) {
+    int j, kq;
+    if (!pslot<N>(jj, j, kq)) continue;
+    int sy, sz, pc;
+    needed_piece<N>(j, sy, sz, pc);
+    double *g = f.u + meta->off[col_sel<N>(sy, sz)] + kq * N3 + sz * NN + sy * N + pc * PW;
+    const double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
+    const bool lastpc = pc == NP - 1;
+    for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) {
+      if (lastpc && k == nk - 1) {
+        if (PW == 2) *g = *sp;  // point n-2; n-1 is the next chunk's seam
+      } else if (PW == 2) {
+        *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(sp);
+      } else {
+        *g = *sp;
+      }
+    }
+  }
+  if ((int)threadIdx.x < NN) {
+    const int r = threadIdx.x, sy = r % N, sz = r / N;
+    f.u[meta->lo[col_sel<N>(sy, sz)] + sz * NN + sy * N + (N - 1)] = buf[K * NN * RS + r];
+  }
+}
+
+}  // namespace ptile
+}  // namespace faces

@@ -37,6 +37,7 @@
 #include "geom.cuh"
 #include "kernels.cuh"
 #include "rows_setup.cuh"
+#include "ptile_steps.cuh"
 #include "tables.h"
 
 void faces_internal_set_error(const char *msg);
@@ -115,6 +116,7 @@ struct faces_server {
   char *d_tables = nullptr;
   size_t tables_fbytes = 0;
   int nunits = 0;
+  int kmode = 0;  // batch_mode of the running set
   long grid = 0;
   Tick ticks[kDepth];
   int tick_head = 0, in_flight = 0;  // ring of in-flight ticks
@@ -292,7 +294,7 @@ int rebuild_tables(faces_server *s, Tick &t)
   for (long long id : order) {
     const Job &job = s->jobs[id];
     append_units(units, (int)fields.size(), job.p, 1);
-    fields.push_back({job.f, job.p});
+    fields.push_back({job.f, job.p, ptile_field(job.f) ? 1 : 0});
   }
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;
   const size_t bytes = fbytes + units.size() * sizeof(BatchUnit);
@@ -314,6 +316,7 @@ int rebuild_tables(faces_server *s, Tick &t)
   CUDA_TRY(cudaMemcpyAsync(s->d_tables, t.staging, bytes, cudaMemcpyHostToDevice, s->stream),
            "server: work list upload");
   s->tables_fbytes = fbytes;
+  s->kmode = batch_mode(fields.data(), fields.size());
   s->nunits = (int)units.size();
   s->grid = std::min<long>((long)s->sms * s->per_sm, std::max(1, s->nunits));
   s->set_changed = false;
@@ -336,7 +339,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          s->stream),
+                          s->kmode, s->stream),
              "server: batched launch");
     s->launches++;
   }

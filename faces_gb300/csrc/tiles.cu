@@ -13,6 +13,7 @@
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
 #include "tile_steps.cuh"
+#include "ptile_steps.cuh"
 
 namespace faces {
 
@@ -86,6 +87,52 @@ __global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
   }
 }
 
+// The periodic tile step (ptile_steps.cuh): the same pipeline with row
+// sources computed from four column offsets per tile.
+template <int N, int K, int NS>
+__global__ void __launch_bounds__(256, 3) ptile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
+  PMeta *meta = reinterpret_cast<PMeta *>(sm + NS * stage);
+  int4 *tinfo = reinterpret_cast<int4 *>(meta + NS);
+  TileWalk nw;
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    // the staged tile, its infos, and the end of the previous tile's store
+    __syncthreads();
+    const int nk = tinfo[s].y;
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = sm + s * stage;
+    sum_tile<N, K>(buf, nullptr, nk, false, true);
+    __syncthreads();
+    ptile::pstore<N, K>(f, buf, meta + s, nk);
+    s = (s + 1) % NS;
+  }
+}
+
 bool tile_kernel_supported(int n) { return n >= 2 && n <= 12; }
 
 int tile_default_chunk(int n) { return tile_kmax(n); }
@@ -102,58 +149,71 @@ size_t tile_smem_bytes(int n, int chunk)
 }
 
 template <int N, int K>
-static cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+static cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
 {
   static_assert(tile_stage_size<N, K>() * sizeof(double) % 16 == 0, "stage alignment");
-  const size_t smem = tile_smem_bytes(N, K);
-  // the attribute is set once per process (one device per process)
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(tile_kernel<N, K, kTileStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
   if (grid > p.ntiles) grid = p.ntiles;
   if (grid < 1) return cudaSuccess;
-  tile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  if (general || !ptile_field(f)) {
+    const size_t smem = tile_smem_bytes(N, K);
+    // the attribute is set once per process (one device per process)
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(tile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    tile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  } else {
+    const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() +
+                        (sizeof(PMeta) + sizeof(int4)) * kTileStages;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(ptile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    ptile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  }
   return cudaGetLastError();
 }
 
 template <int N>
-static cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+static cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
 {
   constexpr int KM = tile_kinst_max(N);
   if (p.chunk > KM) return cudaErrorInvalidValue;
   switch (tile_instance_k(p.chunk)) {
-    case 1: return launch_tiles_nk<N, 1>(f, p, grid, s);
-    case 2: return launch_tiles_nk<N, 2>(f, p, grid, s);
-    case 4: return launch_tiles_nk<N, 4>(f, p, grid, s);
-    case 8: return launch_tiles_nk<N, 8>(f, p, grid, s);
+    case 1: return launch_tiles_nk<N, 1>(f, p, grid, general, s);
+    case 2: return launch_tiles_nk<N, 2>(f, p, grid, general, s);
+    case 4: return launch_tiles_nk<N, 4>(f, p, grid, general, s);
+    case 8: return launch_tiles_nk<N, 8>(f, p, grid, general, s);
     case 16:
-      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, s);
+      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, general, s);
       return cudaErrorInvalidValue;
     case 32:
-      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, s);
+      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, general, s);
       return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general)
 {
   switch (f.n) {
-    case 2: return launch_tiles_n<2>(f, p, grid, s);
-    case 3: return launch_tiles_n<3>(f, p, grid, s);
-    case 4: return launch_tiles_n<4>(f, p, grid, s);
-    case 5: return launch_tiles_n<5>(f, p, grid, s);
-    case 6: return launch_tiles_n<6>(f, p, grid, s);
-    case 7: return launch_tiles_n<7>(f, p, grid, s);
-    case 8: return launch_tiles_n<8>(f, p, grid, s);
-    case 9: return launch_tiles_n<9>(f, p, grid, s);
-    case 10: return launch_tiles_n<10>(f, p, grid, s);
-    case 11: return launch_tiles_n<11>(f, p, grid, s);
-    case 12: return launch_tiles_n<12>(f, p, grid, s);
+    case 2: return launch_tiles_n<2>(f, p, grid, general, s);
+    case 3: return launch_tiles_n<3>(f, p, grid, general, s);
+    case 4: return launch_tiles_n<4>(f, p, grid, general, s);
+    case 5: return launch_tiles_n<5>(f, p, grid, general, s);
+    case 6: return launch_tiles_n<6>(f, p, grid, general, s);
+    case 7: return launch_tiles_n<7>(f, p, grid, general, s);
+    case 8: return launch_tiles_n<8>(f, p, grid, general, s);
+    case 9: return launch_tiles_n<9>(f, p, grid, general, s);
+    case 10: return launch_tiles_n<10>(f, p, grid, general, s);
+    case 11: return launch_tiles_n<11>(f, p, grid, general, s);
+    case 12: return launch_tiles_n<12>(f, p, grid, general, s);
     default: return cudaErrorInvalidValue;
   }
 }

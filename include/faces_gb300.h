@@ -50,6 +50,9 @@ extern "C" {
 #define FACES_GATHER 0x4u   /* force the generic one-thread-per-point kernel */
 #define FACES_ROWS 0x8u     /* use the register row kernel instead of the
                                shared-memory tile kernel */
+#define FACES_GENERAL 0x10u /* periodic direct-mode fields: use the general
+                               tile step instead of the periodic one (same
+                               result; for comparison) */
 
 typedef struct faces_ctx faces_ctx;
 

@@ -146,3 +146,25 @@ def test_many_fields(faces_lib):
     assert info["fused_fields"] == 512
     bad = [i for i, (a, b) in enumerate(zip(ref, got)) if not np.array_equal(a, b)]
     assert not bad, [mix[i] for i in bad[:5]]
+
+
+def test_all_periodic_batch_equals_general_step(faces_lib):
+    """A batch of periodic direct-mode fields runs the periodic tile step
+    only; it must equal the general tile step of each field alone."""
+    F = faces_lib
+    rng = np.random.default_rng(11)
+    mix = []
+    for _ in range(40):
+        L = tuple(int(x) for x in rng.integers(1, 3, size=3))
+        m = tuple(int(x) for x in rng.integers(1, 9, size=3))
+        mix.append((L + m + (int(rng.integers(2, 11)),), True, False))
+    got, info = batched(F, mix, 3, "graph", seed0=500)
+    assert info["fused_fields"] == len(mix)
+    for i, ((shape, _, _), out) in enumerate(zip(mix, got)):
+        f = F.Faces(*shape, periodic=True, general=True)
+        u = f.field()
+        f.init_int(u, 500 + i)
+        f.share_n(u, 3)
+        torch.cuda.synchronize()
+        assert np.array_equal(u.cpu().numpy(), out), f"field {i} {shape}"
+        f.close()

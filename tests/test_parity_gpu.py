@@ -17,9 +17,10 @@ if not torch.cuda.is_available():
     pytest.skip("no CUDA device", allow_module_level=True)
 
 
-def run_gpu(F, s, *, periodic, messages, gather=False, rows=False, init="int", seed=5, nsteps=2, compute=True):
+def run_gpu(F, s, *, periodic, messages, gather=False, rows=False, general=False, init="int", seed=5, nsteps=2,
+            compute=True):
     f = F.Faces(s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n, periodic=periodic, messages=messages, gather=gather,
-                rows=rows)
+                rows=rows, general=general)
     u = f.field()
     if init == "int":
         f.init_int(u, seed)
@@ -54,13 +55,17 @@ SHAPES = [
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
 @pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
-@pytest.mark.parametrize("kernel", ["tiles", "rows"])
+@pytest.mark.parametrize("kernel", ["tiles", "general", "rows"])
 def test_step_bit_exact(oracle, faces_lib, shape, periodic, messages, kernel):
+    """tiles: the periodic tile step where it applies (periodic direct mode),
+    else the general one; general: the general tile step everywhere."""
     O, F = oracle, faces_lib
+    if kernel == "general" and not (periodic and not messages):
+        pytest.skip("same kernel as 'tiles' here")
     s = O.Shape(*shape, periodic=periodic)
     for init in ("int", "ref"):
-        u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, rows=kernel == "rows", init=init,
-                                   nsteps=3)
+        u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, rows=kernel == "rows",
+                                   general=kernel == "general", init=init, nsteps=3)
         ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
         assert np.array_equal(u_init, ref0), "device init differs from the host formula"
         exp = O.groups_share(s, ref0.copy(), True, 3)
@@ -99,14 +104,14 @@ def test_mugs_bit_exact_single_rank(oracle, faces_lib):
     assert np.array_equal(out, O.mugs_share(s, O.init_ref(s), True, 4))
 
 
-@pytest.mark.parametrize("chunk", [1, 2, 3, 5, 8])
-@pytest.mark.parametrize("kernel", ["tiles", "rows"])
+@pytest.mark.parametrize("chunk", [1, 2, 3, 5, 8, 16])
+@pytest.mark.parametrize("kernel", ["tiles", "general", "rows"])
 def test_chunking(oracle, faces_lib, chunk, kernel):
     O, F = oracle, faces_lib
     for periodic, messages in itertools.product([False, True], [False, True]):
         s = O.Shape(2, 1, 1, 7, 2, 2, 5, periodic=periodic)
         f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages,
-                    rows=kernel == "rows")
+                    rows=kernel == "rows", general=kernel == "general")
         f.set_tuning(chunk=chunk, width=1 + chunk % 3, order=[0, 1, 2, 2 + 16][chunk % 4])
         u = f.field()
         f.init_ref(u)
