@@ -203,10 +203,15 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
       cp_commit();
     }
     double *buf = m.data + (long)s * kStage;
+    // periodic step: x pairs, barrier, y/z pairs (each storing its finals);
+    // general step: sums (with their own barriers), barrier, store
     if (nk > 0) {
       switch (n) {
-#define FACES_BSUM(NV) \
-  case NV: sum_tile<NV, bk(NV)>(buf, rfl, nk, hx, regular != 0); break;
+#define FACES_BSUM(NV)                                                       \
+  case NV:                                                                   \
+    if (lean) ptile::pxpass<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk); \
+    else sum_tile<NV, bk(NV)>(buf, rfl, nk, hx, regular != 0);               \
+    break;
         FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
         FACES_BSUM(9) FACES_BSUM(10)
 #undef FACES_BSUM
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
 #define FACES_BSTORE(NV)                                                                                  \
   case NV:                                                                                                 \
     if (lean)                                                                                              \
-      ptile::pstore<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk);                                      \
+      ptile::pyzpass<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk);                                     \
     else                                                                                                   \
       store_tile<NV, bk(NV), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;

@@ -158,36 +158,90 @@ __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, con
   cp_commit();
 }
 
-// Store the changed points: the staged pieces, all but the last element's
-// point n-1 (the next chunk's seam), and the x-lower ends.
+// Sums of a staged tile, each final value stored as soon as it is known:
+//   pxpass  -- x pairs (element k-1 at n-1, or the x-lower end, with element
+//              k at 0) on every row; an interior row's pair is final there;
+//   pyzpass -- after a barrier: y pairs of rows (0, o), (n-1, o) and z pairs
+//              of rows (o, 0), (o, n-1) for o in 1..n-2, and the four corner
+//              rows (y pairs, then z pairs), column by column.  These cells
+//              are disjoint, so one phase does them all.
+// The order is the general step's (x, then y, then z pairs) and every stored
+// cell is one the general step stores, without the unchanged ones.
 template <int N, int K>
-__device__ __forceinline__ void pstore(const FieldDesc &f, const double *buf, const PMeta *meta, int nk)
+__device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PMeta *meta, int nk)
 {
-  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
-  constexpr int KT = PSlots<N>::KT, SPT = PSlots<N>::SPT;
+  constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
-#pragma unroll
-  for (int jj = 0; jj < SPT; jj++) {
-    int j, kq;
-    if (!pslot<N>(jj, j, kq)) continue;
-    int sy, sz, pc;
-    needed_piece<N>(j, sy, sz, pc);
-    double *g = f.u + meta->off[col_sel<N>(sy, sz)] + kq * N3 + sz * NN + sy * N + pc * PW;
-    const double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
-    const bool lastpc = pc == NP - 1;
-    for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) {
-      if (lastpc && k == nk - 1) {
-        if (PW == 2) *g = *sp;  // point n-2; n-1 is the next chunk's seam
-      } else if (PW == 2) {
-        *reinterpret_cast<double2 *>(g) = *reinterpret_cast<const double2 *>(sp);
-      } else {
-        *g = *sp;
-      }
+  double *locol = buf + K * NN * RS;
+  const int items = nk * NN;
+  for (int i = threadIdx.x; i < items; i += blockDim.x) {
+    const int k = i / NN, r = i - k * NN;
+    double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (N - 1);
+    double *hi = buf + (k * NN + r) * RS;
+    const double s = *lo + *hi;
+    *lo = s;
+    *hi = s;
+    const int sy = r % N, sz = r / N;
+    if (sy >= 1 && sy <= N - 2 && sz >= 1 && sz <= N - 2) {
+      // interior rows lie in column 0 (the tile's own elements)
+      double *g = f.u + meta->off[0] + k * N3 + sz * NN + sy * N;
+      g[0] = s;
+      if (k == 0) f.u[meta->lo[0] + sz * NN + sy * N + (N - 1)] = s;
+      else g[-N3 + (N - 1)] = s;
     }
   }
-  if ((int)threadIdx.x < NN) {
-    const int r = threadIdx.x, sy = r % N, sz = r / N;
-    f.u[meta->lo[col_sel<N>(sy, sz)] + sz * NN + sy * N + (N - 1)] = buf[K * NN * RS + r];
+}
+
+template <int N, int K>
+__device__ __forceinline__ void pyzpass(const FieldDesc &f, const double *buf, const PMeta *meta, int nk)
+{
+  constexpr int NN = N * N, RS = smem_row_stride(N);
+  constexpr long N3 = (long)N * N * N;
+  constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
+  const double *locol = buf + K * NN * RS;
+  const int last_c = (nk - 1) * N + (N - 1);  // the next chunk's seam: not stored
+  for (int i = threadIdx.x; i < G * COLS; i += blockDim.x) {
+    const int g = i / COLS, c = i - g * COLS;
+    const double *sb;
+    int srs;
+    long gcol;  // offset of the column within its row, and which offsets table
+    bool lo = false;
+    if (c < K * N) {
+      const int k = c / N, x = c - k * N;
+      if (k >= nk) continue;
+      sb = buf + k * NN * RS + x;
+      srs = RS;
+      gcol = k * N3 + x;
+    } else {
+      sb = locol;
+      srs = 1;
+      gcol = N - 1;
+      lo = true;
+    }
+    const bool store = lo || c != last_c;
+    const long *offs = lo ? meta->lo : meta->off;
+    auto gaddr = [&](int sy, int sz) { return f.u + offs[col_sel<N>(sy, sz)] + gcol + sz * NN + sy * N; };
+    if (g < 2 * (N - 2)) {
+      int ay, az, by, bz;
+      if (g < N - 2) { ay = N - 1; by = 0; az = bz = 1 + g; }              // y pair
+      else { ay = by = 1 + g - (N - 2); az = N - 1; bz = 0; }              // z pair
+      const double s = sb[(az * N + ay) * srs] + sb[(bz * N + by) * srs];
+      if (store) {
+        *gaddr(ay, az) = s;
+        *gaddr(by, bz) = s;
+      }
+    } else {
+      const double c00 = sb[0], c10 = sb[(N - 1) * srs];
+      const double c01 = sb[(N - 1) * N * srs], c11 = sb[(NN - 1) * srs];
+      const double y0 = c10 + c00, y1 = c11 + c01;
+      const double s = y1 + y0;
+      if (store) {
+        *gaddr(0, 0) = s;
+        *gaddr(N - 1, 0) = s;
+        *gaddr(0, N - 1) = s;
+        *gaddr(N - 1, N - 1) = s;
+      }
+    }
   }
 }
 

@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(256, 3) ptile_kernel(FieldDesc f, RowPlan p)
       cp_commit();
     }
     double *buf = sm + s * stage;
-    sum_tile<N, K>(buf, nullptr, nk, false, true);
+    ptile::pxpass<N, K>(f, buf, meta + s, nk);
     __syncthreads();
-    ptile::pstore<N, K>(f, buf, meta + s, nk);
+    ptile::pyzpass<N, K>(f, buf, meta + s, nk);
     s = (s + 1) % NS;
   }
 }
