@@ -67,6 +67,10 @@ def lib() -> ctypes.CDLL:
     L.faces_run_host.argtypes = [vp, dp, dp, c_int, c_int, vp]
     L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
+    L.faces_autotune.argtypes = [vp, dp, c_int, c_int, vp]
+    L.faces_autotune.restype = c_int
+    L.faces_get_tuning.argtypes = [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    L.faces_get_tuning.restype = c_int
     L.faces_last_error.restype = ctypes.c_char_p
     ip = ctypes.POINTER(c_int)
     L.faces_batch_create.argtypes = [ctypes.POINTER(vp)]
@@ -291,6 +295,17 @@ class Faces:
         kernel: resident blocks per SM) and tile order (0 strided, 1
         contiguous); 0 / -1 keep the defaults."""
         _check(lib().faces_set_tuning(self._h, chunk, width, order))
+
+    def autotune(self, u, compute: bool = True, trials: int = 3, stream=None) -> int:
+        """Keeps the fastest tile settings for this field; returns the shares
+        its timed launches applied to u (re-initialise u afterwards)."""
+        return _check(lib().faces_autotune(self._h, _ptr(u), int(compute), trials, _stream(stream)))
+
+    def tuning(self) -> dict:
+        """The tile step's settings: elements per tile, chunks per unit, blocks."""
+        v = [ctypes.c_int() for _ in range(3)]
+        _check(lib().faces_get_tuning(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("chunk", "unit_chunks", "blocks"), (x.value for x in v)))
 
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))

@@ -520,7 +520,7 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
   int best_div = b->unit_div, best_sm = b->per_sm;
   int applied = 0;  // shares the timed launches applied to each batched field
   int rc = FACES_OK;
-  const int divs[] = {1, 2, 4, 8};
+  const int divs[] = {1, 2, 4, 8, 64};
   for (int d : divs) {
     for (int sm = fit; sm >= std::max(1, fit - 1) && rc == FACES_OK; sm--) {
       b->unit_div = d;

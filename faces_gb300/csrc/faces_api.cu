@@ -226,6 +226,15 @@ int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
   return FACES_OK;
 }
 
+int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (chunk) *chunk = c->tplan.chunk;
+  if (unit_chunks) *unit_chunks = c->tplan.unit_chunks;
+  if (blocks) *blocks = (int)c->tgrid;
+  return FACES_OK;
+}
+
 int faces_launches_per_share(const faces_ctx *c, int compute)
 {
   if (int rc = check_ctx(c)) return rc;
@@ -262,6 +271,56 @@ int faces_share_n(faces_ctx *c, double *u, int compute, int nshares, void *strea
   for (int i = 0; i < nshares; i++)
     if (int rc = share_once(c, u, compute, static_cast<cudaStream_t>(stream))) return rc;
   return FACES_OK;
+}
+
+int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (!u) return fail(FACES_EINVAL, "null field");
+  if (trials < 1) trials = 3;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!(compute && !(c->flags & (FACES_GATHER | FACES_ROWS)) && tile_kernel_supported(c->n))) return 0;
+  // candidates: elements per tile (default, half, double), units of one
+  // chunk or half a column (order 2 + 16*u), resident blocks per SM
+  const int k0 = c->tplan.chunk;
+  const int ks[3] = {k0, k0 / 2, k0 * 2};
+  const int orders[2] = {-1, 2 + 16};
+  const int widths[2] = {0, 2};
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
+  CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
+  float best = 1e30f;
+  int bk = c->chunk, bo = c->order, bw = c->tpb, applied = 0, rc = FACES_OK;
+  for (int ki = 0; ki < 3 && rc == FACES_OK; ki++) {
+    if (ks[ki] < 1 || (ki > 0 && ks[ki] == k0)) continue;
+    for (int o : orders)
+      for (int w : widths) {
+        if (rc != FACES_OK) break;
+        c->chunk = ks[ki];
+        c->order = o;
+        c->tpb = w;
+        replan(*c);
+        if (ki == 2 && c->tplan.chunk == k0) continue;  // doubling not possible
+        if ((rc = share_once(c, u, compute, s))) break;  // warm-up
+        cudaEventRecord(e0, s);
+        for (int t = 0; t < trials && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
+        cudaEventRecord(e1, s);
+        applied += 1 + trials;
+        if (rc) break;
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) { rc = fail(FACES_ECUDA, "autotune: %s", cudaGetErrorString(e)); break; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; bk = c->chunk; bo = c->order; bw = c->tpb; }
+      }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->chunk = bk;
+  c->order = bo;
+  c->tpb = bw;
+  replan(*c);
+  return rc ? rc : applied;
 }
 
 int faces_init_ref(faces_ctx *c, double *u, void *stream)

@@ -66,6 +66,8 @@ int fail(int code, const char *fmt, ...)
   } while (0)
 
 constexpr int kDepth = 2;  // ticks in flight
+// work units of one x-chunk each (units of a job listed chunk group first)
+constexpr int kServeUnitDiv = 64;
 
 enum JobState { kQueued = 0, kRunning = 1, kDone = 2, kReleased = 3 };
 
@@ -181,7 +183,7 @@ void plain_plan(faces_server *s, Job &job)
   const int n = job.f.n;
   job.tp = make_row_plan(job.f, tile_default_chunk(n), 0);
   job.tp.order = 2;
-  job.tp.unit_chunks = (job.tp.nchunks + 1) / 2;
+  job.tp.unit_chunks = ptile_field(job.f) ? 1 : (job.tp.nchunks + 1) / 2;
   int fit = (int)((228 * 1024) / (tile_smem_bytes(n, job.tp.chunk) + 1024));
   fit = std::max(1, std::min(8, fit));
   job.tgrid = (long)s->sms * fit;
@@ -293,7 +295,7 @@ int rebuild_tables(faces_server *s, Tick &t)
   fields.reserve(order.size());
   for (long long id : order) {
     const Job &job = s->jobs[id];
-    append_units(units, (int)fields.size(), job.p, 1);
+    append_units(units, (int)fields.size(), job.p, kServeUnitDiv);
     fields.push_back({job.f, job.p, ptile_field(job.f) ? 1 : 0});
   }
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;

@@ -114,8 +114,22 @@ int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int comput
  * block for the row kernel, resident blocks per SM for the tile kernel, and
  * the tile kernel's order (< 0: default = 2, 0: blocks stride over the tiles,
  * 1: each block takes a contiguous range of x-chunks, 2 + 16*u: blocks stride
- * over units of u consecutive x-chunks of a column, u = 0 half a column). */
+ * over units of u consecutive x-chunks of a column, listed chunk group first;
+ * u = 0: one chunk for the periodic step, half a column otherwise). */
 int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
+
+/* Times the tile step on the field u over elements per tile (default, half,
+ * double), units (half a column, one chunk) and resident blocks per SM
+ * (default, 2), `trials` shares each after one warm-up, and keeps the
+ * fastest (faces_set_tuning's settings).  Every timed launch is a share of
+ * u: returns how many it applied (>= 0; re-initialise u afterwards) or an
+ * error code.  The reference fixes these choices at compile time
+ * (MAXTHREADS, gpu/gpu.h:185-200).  Synchronous. */
+int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *stream);
+
+/* The tile step's current settings: elements per tile, x-chunks per unit
+ * of work, blocks launched.  Any pointer may be NULL. */
+int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks);
 
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);
@@ -181,7 +195,7 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream);
  * x-chunks; <= 0 keeps it) and resident blocks per SM (<= 0 keeps it). */
 int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm);
 
-/* Times the batched launch over unit_div in {1,2,4,8} and the resident
+/* Times the batched launch over unit_div in {1,2,4,8,64} and the resident
  * blocks per SM that fit, `trials` launches each (after one warm-up), and
  * keeps the fastest.  Every launch is a share of the fields in the batched
  * launch (the others are untouched): returns how many shares it applied to

@@ -137,3 +137,25 @@ def test_large_field_properties(oracle, faces_lib, kernel):
         outs.append(u)
         f.close()
     assert torch.equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1, 9, 7, 5, 8), (2, 1, 2, 5, 3, 4, 5), (1, 2, 1, 6, 4, 3, 10)],
+                         ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+def test_autotune_keeps_results(oracle, faces_lib, shape, periodic):
+    """faces_autotune times several tile settings on the field and keeps one;
+    every setting it can pick must give the oracle's result."""
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=periodic)
+    f = F.Faces(*shape, periodic=periodic)
+    u = f.field()
+    f.init_int(u, 5)
+    applied = f.autotune(u, trials=1)
+    assert applied >= 4
+    t = f.tuning()
+    assert t["chunk"] >= 1 and t["unit_chunks"] >= 1 and t["blocks"] >= 1
+    f.init_int(u, 5)
+    f.share_n(u, 3)
+    torch.cuda.synchronize()
+    assert np.array_equal(u.cpu().numpy(), O.groups_share(s, O.init_int(s, 5), True, 3))
+    f.close()
