@@ -14,7 +14,7 @@ value     = whole-job HBM GB/s: algorithmic bytes (each field point read and
 e2e       = the same metric through the C ABI from pinned host memory: each
             e2e step is the configuration's job -- upload the field, 100 shares
             (ni = 100), download the result -- via faces_run_host
-roofline  = the row kernel against MEASURED_PEAKS.json's copy bandwidth
+roofline  = the periodic tile kernel against MEASURED_PEAKS.json's copy bandwidth
 cpu_baseline = the reference's v-26 pack/inner/unpack loops transcribed to
             host C with OpenMP (the oracle), timed on this host's cores
 
@@ -54,7 +54,7 @@ E2E_SHARES = 100  # ni of the configuration (nk=1 nj=1 ni=100)
 # shares; here the re-init runs INSIDE the timed region and counts against
 # the result.
 RESEED_EVERY = 100
-KERNEL_NAME = "faces::tile_kernel<8,4,3>"
+KERNEL_BASE = "faces::ptile_kernel<8,{k},3>"  # the periodic tile step, n = 8, K elements per tile
 L2_BYTES = 126 * 2 ** 20
 
 
@@ -166,9 +166,9 @@ def hbm_peak() -> tuple[float, str]:
 
 
 def profiled_traffic() -> float | None:
-    """dram bytes per launch of the row kernel on this workload, from the
-    committed ncu summary (profiles/tile_kernel_n8_48cubed.txt)."""
-    path = os.path.join(ROOT, "profiles", "tile_kernel_n8_48cubed.txt")
+    """dram bytes per launch of the periodic tile kernel on this workload,
+    from the committed ncu summary (profiles/ptile_kernel_n8_48cubed.txt)."""
+    path = os.path.join(ROOT, "profiles", "ptile_kernel_n8_48cubed.txt")
     try:
         with open(path) as fh:
             for line in fh:
@@ -314,7 +314,7 @@ def run_faces(args) -> dict | None:
         "points_per_s": round(world * points * args.steps / t_max, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
-                     "kernel": KERNEL_NAME,
+                     "kernel": KERNEL_BASE.format(k=1 << max(0, (tuned["chunk"] - 1).bit_length())),
                      "algorithmic_bytes_per_launch": bytes_step,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
         "clocks": clocks,
@@ -470,6 +470,26 @@ def served_leg(F) -> dict:
     }
 
 
+def profile_c4(F, shares: int) -> dict:
+    """The 512-field batch with default settings, `shares` batched shares
+    (no autotune, no graph): the case the batched kernel is profiled on."""
+    import torch
+    fields = []
+    for i, sh in enumerate(c4_mix()):
+        f = F.Faces(*sh, periodic=True)
+        u = f.field()
+        f.init_int(u, 100 + i)
+        fields.append((f, u))
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    for _ in range(shares):
+        b.share()
+    torch.cuda.synchronize()
+    return {"case": "c4", "shares": shares, "batch": b.info()}
+
+
 def run_reference(args) -> dict | None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -502,8 +522,14 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--profile-c4", type=int, default=0, metavar="N",
+                    help="only build the 512-field batch and run N batched shares (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_c4:
+        import faces_gb300 as F
+        print(json.dumps(profile_c4(F, args.profile_c4)), flush=True)
+        return
     out = run_reference(args) if args.impl == "reference" else run_faces(args)
     if out is not None:
         print(json.dumps(out), flush=True)
