@@ -27,6 +27,7 @@ MESSAGES = 0x2
 GATHER = 0x4
 ROWS = 0x8
 GENERAL = 0x10
+V6 = 0x20
 
 _ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
 
@@ -196,19 +197,21 @@ class Faces:
     gather   -- force the generic one-thread-per-point kernel
     rows     -- use the register row kernel instead of the shared-memory tiles
     general  -- periodic fields: the general tile step instead of the periodic one
+    v6       -- v-6 strategy: six face messages per rank, sweeps z, y, x
+                (gpu/v-6-messages-basic/Faces.cc:65-173)
     """
 
     def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
                  periodic: bool = False, messages: bool = False, gather: bool = False, rows: bool = False,
-                 general: bool = False):
+                 general: bool = False, v6: bool = False):
         flags = ((PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
-                 | (ROWS if rows else 0) | (GENERAL if general else 0))
+                 | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0))
         h = ctypes.c_void_p()
         _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
         self._h = h
         self.shape = (lx, ly, lz, mx, my, mz, n)
         self.periodic, self.messages, self.gather, self.rows = periodic, messages, gather, rows
-        self.general = general
+        self.general, self.v6 = general, v6
         s = (ctypes.c_long * 6)()
         rd, tot = ctypes.c_long(), ctypes.c_long()
         _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
@@ -332,7 +335,7 @@ class Batch:
         lx, ly, lz, mx, my, mz, n = faces.shape
         flags = ((PERIODIC if faces.periodic else 0) | (MESSAGES if faces.messages else 0)
                  | (GATHER if faces.gather else 0) | (ROWS if faces.rows else 0)
-                 | (GENERAL if faces.general else 0))
+                 | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0))
         fid = ctypes.c_int()
         _check(lib().faces_batch_add(self._h, _ptr(u), lx, ly, lz, mx, my, mz, n, flags, ctypes.byref(fid)))
         self._fields.append(u)

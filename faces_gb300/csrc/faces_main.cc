@@ -17,6 +17,8 @@
 //   --messages        v-26 strategy: 26 messages per rank, swapped by buffer
 //   --gather          force the generic one-thread-per-point kernel
 //   --rows            use the register row kernel instead of the tile kernel
+//   --v6              v-6 strategy: six face messages per rank, sweeps z, y, x
+//   --general         periodic fields: the general tile step
 //   --init=ref|int    initial state: gpu/main.cc:18 formula (default) or
 //                     integer values from --seed=S
 //   --chunk=K --tpb=T --order=O   work decomposition (faces_set_tuning)
@@ -71,6 +73,8 @@ int main(int argc, char *argv[])
     else if (s == "--messages") flags |= FACES_MESSAGES;
     else if (s == "--gather") flags |= FACES_GATHER;
     else if (s == "--rows") flags |= FACES_ROWS;
+    else if (s == "--v6") flags |= FACES_V6;
+    else if (s == "--general") flags |= FACES_GENERAL;
     else if (s == "--json") json = true;
     else if (s == "--init=ref") init = 0;
     else if (s == "--init=int") init = 1;

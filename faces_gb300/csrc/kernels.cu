@@ -535,6 +535,123 @@ cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStr
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// v-6 (gpu/v-6-messages-basic/Faces.cc:65-173): six face messages per rank
+// and three dimension sweeps, z then y then x.  Face d of a rank holds the
+// n*n*m_a*m_b points of its low (i_d = 0, j_d = 0) or high (i_d = n-1,
+// j_d = m_d-1) plane, a < b the other two dimensions, point (ia, ib, ja, jb)
+// at ia + n*ib + n^2*ja + n^2*m_a*jb (the layout of zfs(ix,iy,jx,jy),
+// yfs(ix,iz,jx,jz), xfs(iy,iz,jy,jz)).  Per rank the buffer holds the x, y, z
+// faces, low then high.
+// ---------------------------------------------------------------------------
+
+struct V6Geom {
+  int d, a, b;
+  long F, per_rank, off;  // face doubles, doubles per rank, offset of dimension d
+};
+
+V6Geom v6_geom(const FieldDesc &f, int d)
+{
+  V6Geom g;
+  g.d = d;
+  g.a = d == 0 ? 1 : 0;
+  g.b = d == 2 ? 1 : 2;
+  const long nn = (long)f.n * f.n;
+  const long Fd[3] = {nn * f.m[1] * f.m[2], nn * f.m[0] * f.m[2], nn * f.m[0] * f.m[1]};
+  g.F = Fd[d];
+  g.per_rank = 2 * (Fd[0] + Fd[1] + Fd[2]);
+  g.off = 2 * (d > 0 ? Fd[0] : 0) + 2 * (d > 1 ? Fd[1] : 0);
+  return g;
+}
+
+long v6_message_doubles(const FieldDesc &f) { return v6_geom(f, 0).per_rank * f.nranks; }
+
+__device__ __forceinline__ void v6_point(const FieldDesc &f, const V6Geom &g, long idx, int i[3], int j[3])
+{
+  const int n = f.n;
+  const long nn = (long)n * n, pa = nn * f.m[g.a];
+  const int jb = (int)(idx / pa);
+  long q = idx - (long)jb * pa;
+  const int ja = (int)(q / nn);
+  q -= (long)ja * nn;
+  i[g.b] = (int)(q / n);
+  i[g.a] = (int)(q - (long)i[g.b] * n);
+  j[g.a] = ja;
+  j[g.b] = jb;
+}
+
+// every rank's two faces of dimension d, after the earlier sweeps
+__global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
+{
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= f.nranks * 2 * g.F) return;
+  const int r = (int)(t / (2 * g.F));
+  const long rem = t - (long)r * 2 * g.F;
+  const int side = rem >= g.F;
+  const long idx = rem - side * g.F;
+  int i[3], j[3];
+  v6_point(f, g, idx, i, j);
+  i[g.d] = side ? f.n - 1 : 0;
+  j[g.d] = side ? f.m[g.d] - 1 : 0;
+  msg[(long)r * g.per_rank + g.off + side * g.F + idx] =
+      f.u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+}
+
+// low face += the lower neighbour's high face, element pairs along d, high
+// face += the upper neighbour's low face; compute = 0: element pairs only
+// where the point is on the subdomain boundary in another dimension
+__global__ void v6_update_kernel(FieldDesc f, V6Geom g, const double *msg, int compute)
+{
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= f.nranks * g.F) return;
+  const int r = (int)(t / g.F);
+  const long idx = t - (long)r * g.F;
+  const int n = f.n, d = g.d;
+  int i[3], j[3];
+  v6_point(f, g, idx, i, j);
+  const bool on_a = (i[g.a] == 0 && j[g.a] == 0) || (i[g.a] == n - 1 && j[g.a] == f.m[g.a] - 1);
+  const bool on_b = (i[g.b] == 0 && j[g.b] == 0) || (i[g.b] == n - 1 && j[g.b] == f.m[g.b] - 1);
+  const int dm[3] = {d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0};
+  const int lo = nbr_of(f, r, dir_index(dm[0], dm[1], dm[2]));
+  const int hi = nbr_of(f, r, dir_index(-dm[0], -dm[1], -dm[2]));
+  double *ur = f.u + (long)r * f.R;
+  i[d] = 0;
+  j[d] = 0;
+  if (lo >= 0) {
+    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
+    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + idx];
+  }
+  if (compute || on_a || on_b) {
+    const long sd = d == 0 ? (long)n * n * n : d == 1 ? f.sjy : f.sjz;  // element stride along d
+    const long pd = d == 0 ? 1 : d == 1 ? n : (long)n * n;              // point stride along d
+    i[d] = n - 1;
+    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
+    for (int jd = 0; jd + 1 < f.m[d]; jd++, p += sd) {
+      double *q = p + sd - (long)(n - 1) * pd;
+      const double v = *p + *q;
+      *p = v;
+      *q = v;
+    }
+  }
+  if (hi >= 0) {
+    i[d] = n - 1;
+    j[d] = f.m[d] - 1;
+    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
+    *p = *p + msg[(long)hi * g.per_rank + g.off + idx];
+  }
+}
+
+cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
+{
+  for (int d = 2; d >= 0; d--) {
+    const V6Geom g = v6_geom(f, d);
+    const long np = f.nranks * 2 * g.F, nu = f.nranks * g.F;
+    v6_pack_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+    v6_update_kernel<<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
 {
   long maxsz = 0;

@@ -16,6 +16,11 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s);
 cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s);
 cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 
+// v-6 strategy (FACES_V6): six face messages per rank in `msg`
+// (v6_message_doubles of them), sweeps z, y, x; six launches
+long v6_message_doubles(const FieldDesc &f);
+cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s);
+
 // shared-memory tile step (tiles.cu): chunk (plan.chunk) at most tile_kinst_max(n)
 bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);

@@ -53,6 +53,14 @@ extern "C" {
 #define FACES_GENERAL 0x10u /* periodic direct-mode fields: use the general
                                tile step instead of the periodic one (same
                                result; for comparison) */
+#define FACES_V6 0x20u      /* v-6 strategy (gpu/v-6-messages-basic/Faces.cc:
+                               65-173): six face messages per rank, sweeps z,
+                               then y, then x; each point gets the tree sum in
+                               the order z, y, x pairs (equal to the other
+                               modes on integer inputs, within the reference's
+                               1e-15 check otherwise).  compute = 0 sums only
+                               subdomain-boundary points (the reference's v-6
+                               ignores compute). */
 
 typedef struct faces_ctx faces_ctx;
 

@@ -653,6 +653,108 @@ void orc_v26_share(const orc_geom *g, double *u, int compute, int nsteps, int nt
 }
 
 /* ------------------------------------------------------------------ */
+/* v-6: six face messages, three dimension sweeps                       */
+/* (gpu/v-6-messages-basic/Faces.cc:65-173)                             */
+/* ------------------------------------------------------------------ */
+
+/* point (i, j) of dimension a lies on the subdomain boundary */
+static inline int v6_on_boundary(const geo *o, int a, int i, int j)
+{
+  return (i == 0 && j == 0) || (i == o->n - 1 && j == o->m[a] - 1);
+}
+
+/* One share: sweeps in the reference's order z, y, x.  In the sweep of
+ * dimension d every rank first packs its two face planes (the low face
+ * i_d = 0 of element j_d = 0, the high face i_d = n-1 of element m_d-1;
+ * Faces.cc:89-92,118-121,147-150), then adds to its low face the high face
+ * its lower neighbour packed, sums each pair of neighbouring elements
+ * (element j_d at n-1 with element j_d+1 at 0), and adds to its high face
+ * the low face its upper neighbour packed (Faces.cc:105-113,134-142,
+ * 163-171).  Faces carry the earlier sweeps' sums, so edges and corners
+ * reach every copy: each point ends as the tree z pairs, y pairs, x pairs.
+ * compute = 0 (the reference's v-6 ignores it) sums only points on the
+ * subdomain boundary, as the other strategies do: a pair inside the
+ * subdomain is taken only where its point lies on the boundary in another
+ * dimension. */
+static void v6_step(const geo *o, double *u, int compute, double *send)
+{
+  const int n = o->n;
+  for (int d = 2; d >= 0; d--) {
+    const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+    const long F = (long)n * n * o->m[a] * o->m[b];
+    /* pack: face side s of rank r at send[(r*2 + s)*F + idx] */
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < o->nranks; r++)
+      for (int jb = 0; jb < o->m[b]; jb++)
+        for (int ja = 0; ja < o->m[a]; ja++)
+          for (int ib = 0; ib < n; ib++)
+            for (int ia = 0; ia < n; ia++) {
+              const long idx = ia + (long)n * ib + (long)n * n * ja + (long)n * n * o->m[a] * jb;
+              int i[3], j[3];
+              i[a] = ia; i[b] = ib; j[a] = ja; j[b] = jb;
+              i[d] = 0; j[d] = 0;
+              send[((long)r * 2 + 0) * F + idx] = u[(long)r * o->R + gidx(o, i, j)];
+              i[d] = n - 1; j[d] = o->m[d] - 1;
+              send[((long)r * 2 + 1) * F + idx] = u[(long)r * o->R + gidx(o, i, j)];
+            }
+    /* updates */
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < o->nranks; r++) {
+      int dm[3] = {0, 0, 0}, dp[3] = {0, 0, 0};
+      dm[d] = -1;
+      dp[d] = 1;
+      const int lo = neighbor(o, r, dm), hi = neighbor(o, r, dp);
+      double *ur = u + (long)r * o->R;
+      for (int jb = 0; jb < o->m[b]; jb++)
+        for (int ja = 0; ja < o->m[a]; ja++)
+          for (int ib = 0; ib < n; ib++)
+            for (int ia = 0; ia < n; ia++) {
+              const long idx = ia + (long)n * ib + (long)n * n * ja + (long)n * n * o->m[a] * jb;
+              const int keep = compute || v6_on_boundary(o, a, ia, ja) || v6_on_boundary(o, b, ib, jb);
+              int i[3], j[3];
+              i[a] = ia; i[b] = ib; j[a] = ja; j[b] = jb;
+              if (lo >= 0) {
+                i[d] = 0; j[d] = 0;
+                double *p = ur + gidx(o, i, j);
+                *p = *p + send[((long)lo * 2 + 1) * F + idx];
+              }
+              if (keep)
+                for (int jd = 0; jd + 1 < o->m[d]; jd++) {
+                  i[d] = n - 1; j[d] = jd;
+                  double *p = ur + gidx(o, i, j);
+                  i[d] = 0; j[d] = jd + 1;
+                  double *q = ur + gidx(o, i, j);
+                  const double s = *p + *q;
+                  *p = s;
+                  *q = s;
+                }
+              if (hi >= 0) {
+                i[d] = n - 1; j[d] = o->m[d] - 1;
+                double *p = ur + gidx(o, i, j);
+                *p = *p + send[((long)hi * 2 + 0) * F + idx];
+              }
+            }
+    }
+  }
+}
+
+void orc_v6_share(const orc_geom *g, double *u, int compute, int nsteps)
+{
+  geo o;
+  geo_make(g, &o);
+  long fmax = 0;
+  for (int d = 0; d < 3; d++) {
+    const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+    const long F = (long)o.n * o.n * o.m[a] * o.m[b];
+    if (F > fmax) fmax = F;
+  }
+  double *send = (double *)malloc(sizeof(double) * (size_t)(fmax * 2 * o.nranks));
+  if (!send) return;
+  for (int t = 0; t < nsteps; t++) v6_step(&o, u, compute, send);
+  free(send);
+}
+
+/* ------------------------------------------------------------------ */
 /* correctness check, gpu/main.cc:39-105                                 */
 /* ------------------------------------------------------------------ */
 

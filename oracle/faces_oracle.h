@@ -70,6 +70,9 @@ void orc_groups_share(const orc_geom *g, double *u, int compute, int nsteps);
 void orc_mugs_share(const orc_geom *g, double *u, int compute, int nsteps);
 /* nthreads <= 0: OpenMP default. */
 void orc_v26_share(const orc_geom *g, double *u, int compute, int nsteps, int nthreads);
+/* the v-6 strategy: z, y, x dimension sweeps of face messages and element
+ * pairs (sums in the tree order z, y, x) */
+void orc_v6_share(const orc_geom *g, double *u, int compute, int nsteps);
 
 /* gpu/main.cc:39-105 check on every rank: max relative error
  * |a-b|/(|a|+|b|) (0 where the denominator is <= 1e-15) over the points of

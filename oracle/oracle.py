@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
         L.orc_groups_share.argtypes = [gp, dp, ctypes.c_int, ctypes.c_int]
         L.orc_mugs_share.argtypes = [gp, dp, ctypes.c_int, ctypes.c_int]
         L.orc_v26_share.argtypes = [gp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_v6_share.argtypes = [gp, dp, ctypes.c_int, ctypes.c_int]
         L.orc_compare.argtypes = [gp, dp, dp, ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.orc_compare.restype = ctypes.c_double
@@ -146,6 +147,12 @@ def groups_share(s: Shape, u: np.ndarray, compute: bool = True, nsteps: int = 1)
 
 def mugs_share(s: Shape, u: np.ndarray, compute: bool = True, nsteps: int = 1) -> np.ndarray:
     lib().orc_mugs_share(ctypes.byref(s.geom()), _dp(u), int(compute), nsteps)
+    return u
+
+
+def v6_share(s: Shape, u: np.ndarray, compute: bool = True, nsteps: int = 1) -> np.ndarray:
+    """v-6 (gpu/v-6-messages-basic/Faces.cc:65-173): z, y, x sweeps."""
+    lib().orc_v6_share(ctypes.byref(s.geom()), _dp(u), int(compute), nsteps)
     return u
 
 

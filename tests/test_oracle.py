@@ -112,9 +112,10 @@ def test_formulations_agree(oracle, shape, periodic):
         assert mv < 1e-15
 
 
-def python_share(s, u, compute=True):
+def python_share(s, u, compute=True, order="xyz"):
     """Pure-Python statement of one share on the global mesh (tiny shapes):
-    every global point's copies get the sum x-pairs -> y-pairs -> z-pairs."""
+    every global point's copies get the sum x-pairs -> y-pairs -> z-pairs
+    (order "zyx": z-pairs -> y-pairs -> x-pairs, the v-6 sweeps)."""
     n = s.n
     L, m = (s.lx, s.ly, s.lz), (s.mx, s.my, s.mz)
     M = [L[a] * m[a] for a in range(3)]
@@ -149,14 +150,16 @@ def python_share(s, u, compute=True):
                 span = [m[a] * (n - 1) for a in range(3)]
                 if not compute and all(g % sp for g, sp in zip((gx, gy, gz), span)):
                     continue
-                sz = []
-                for ez in cz:
-                    sy = []
-                    for ey in cy:
-                        vals = [u[addr((ex[0], ey[0], ez[0]), (ex[1], ey[1], ez[1]))] for ex in cx]
-                        sy.append(vals[0] + vals[1] if len(vals) == 2 else vals[0])
-                    sz.append(sy[0] + sy[1] if len(sy) == 2 else sy[0])
-                tot = sz[0] + sz[1] if len(sz) == 2 else sz[0]
+                def pair(v):
+                    return v[0] + v[1] if len(v) == 2 else v[0]
+
+                def val(ex, ey, ez):
+                    return u[addr((ex[0], ey[0], ez[0]), (ex[1], ey[1], ez[1]))]
+
+                if order == "xyz":
+                    tot = pair([pair([pair([val(ex, ey, ez) for ex in cx]) for ey in cy]) for ez in cz])
+                else:
+                    tot = pair([pair([pair([val(ex, ey, ez) for ez in cz]) for ey in cy]) for ex in cx])
                 for ez in cz:
                     for ey in cy:
                         for ex in cx:
@@ -175,6 +178,38 @@ def test_pure_python_restatement(oracle, shape, periodic):
     u0[m] = rng.standard_normal(m.sum())
     for compute in (True, False):
         assert np.array_equal(python_share(s, u0, compute), O.groups_share(s, u0.copy(), compute, 1))
+
+
+@pytest.mark.parametrize("shape,periodic", [((1, 1, 1, 2, 2, 2, 3), True), ((2, 1, 1, 2, 1, 2, 3), False),
+                                            ((1, 2, 2, 1, 2, 1, 4), True), ((2, 2, 2, 1, 1, 1, 2), True),
+                                            ((2, 1, 2, 3, 1, 1, 2), False)])
+def test_v6_restatement(oracle, shape, periodic):
+    """The v-6 sweeps (z, then y, then x) give every point the tree sum in the
+    order z pairs, y pairs, x pairs; on integer inputs that equals every other
+    formulation."""
+    O = oracle
+    s = O.Shape(*shape, periodic=periodic)
+    rng = np.random.default_rng(1)
+    u0 = O.init_int(s, 2)
+    for compute in (True, False):
+        assert np.array_equal(O.v6_share(s, u0.copy(), compute, 3), O.groups_share(s, u0.copy(), compute, 3))
+    m = u0 != 0
+    u1 = u0.copy()
+    u1[m] = rng.standard_normal(m.sum())
+    for compute in (True, False):
+        assert np.array_equal(python_share(s, u1, compute, order="zyx"), O.v6_share(s, u1.copy(), compute, 1))
+
+
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+def test_v6_reference_init_within_check(oracle, periodic):
+    """On the reference's non-integer init the v-6 order differs from Mugs in
+    the last bits only: within the reference's own 1e-15 check."""
+    O = oracle
+    s = O.Shape(2, 2, 1, 3, 2, 4, 5, periodic=periodic)
+    a = O.v6_share(s, O.init_ref(s), True, 3)
+    b = O.mugs_share(s, O.init_ref(s), True, 3)
+    mv, npass, _ = O.compare(s, a, b)
+    assert mv < 1e-15 and npass == s.nranks
 
 
 def test_closed_form_of_repeated_shares(oracle):

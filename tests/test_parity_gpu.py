@@ -159,3 +159,29 @@ def test_autotune_keeps_results(oracle, faces_lib, shape, periodic):
     torch.cuda.synchronize()
     assert np.array_equal(u.cpu().numpy(), O.groups_share(s, O.init_int(s, 5), True, 3))
     f.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+def test_v6_bit_exact(oracle, faces_lib, shape, periodic):
+    """The v-6 strategy (six face messages, sweeps z, y, x) against the
+    oracle's v-6 restatement bit for bit, on both inits and with compute on
+    and off; on integer inputs also against the tree of the other modes."""
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=periodic)
+    for init in ("int", "ref"):
+        for compute in (True, False):
+            f = F.Faces(*shape, periodic=periodic, v6=True)
+            assert f.launches_per_share() == 6
+            u = f.field()
+            f.init_int(u, 5) if init == "int" else f.init_ref(u)
+            f.share_n(u, 3, compute)
+            chk = f.check(u, init=init, seed=5, nshares=3, compute=compute)
+            torch.cuda.synchronize()
+            out = u.cpu().numpy()
+            f.close()
+            ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
+            assert np.array_equal(out, O.v6_share(s, ref0.copy(), compute, 3)), (init, compute)
+            if init == "int":
+                assert np.array_equal(out, O.groups_share(s, ref0.copy(), compute, 3))
+            assert chk.passed, (init, compute, chk.maxrel)
