@@ -94,8 +94,8 @@ void replan(faces_ctx &c)
     c.tplan.unit_chunks = uc < 1 ? 1 : uc;
     // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved
     // per block) and 2048 threads of 256-thread blocks
-    int fit = (int)((228 * 1024) / (tile_smem_bytes(c.n, k) + 1024));
-    if (fit > 8) fit = 8;
+    const bool periodic_step = (c.flags & FACES_PERIODIC) && !(c.flags & (FACES_MESSAGES | FACES_GENERAL));
+    const int fit = tile_blocks_per_sm(c.n, k, periodic_step);
     const int per_sm = c.tpb > 0 ? (c.tpb < fit ? c.tpb : fit) : fit;
     c.tgrid = (long)c.sms * (per_sm < 1 ? 1 : per_sm);
   }

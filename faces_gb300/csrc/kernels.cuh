@@ -25,6 +25,7 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
 bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);
 size_t tile_smem_bytes(int n, int chunk);
+int tile_blocks_per_sm(int n, int chunk, bool periodic_step);
 // periodic direct-mode fields take the periodic tile step unless `general`
 cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false);
 

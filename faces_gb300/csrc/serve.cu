@@ -184,9 +184,7 @@ void plain_plan(faces_server *s, Job &job)
   job.tp = make_row_plan(job.f, tile_default_chunk(n), 0);
   job.tp.order = 2;
   job.tp.unit_chunks = ptile_field(job.f) ? 1 : (job.tp.nchunks + 1) / 2;
-  int fit = (int)((228 * 1024) / (tile_smem_bytes(n, job.tp.chunk) + 1024));
-  fit = std::max(1, std::min(8, fit));
-  job.tgrid = (long)s->sms * fit;
+  job.tgrid = (long)s->sms * tile_blocks_per_sm(n, job.tp.chunk, ptile_field(job.f));
 }
 
 int admit(faces_server *s, Job &job)

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
 // The periodic tile step (ptile_steps.cuh): the same pipeline with row
 // sources computed from four column offsets per tile.
 template <int N, int K, int NS>
-__global__ void __launch_bounds__(256, 3) ptile_kernel(FieldDesc f, RowPlan p)
+__global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
 {
   constexpr int stage = tile_stage_size<N, K>();
   extern __shared__ __align__(16) double sm[];
@@ -146,6 +146,19 @@ size_t tile_smem_bytes(int n, int chunk)
   return sizeof(double) * (kTileStages * tile_stage_doubles(n, K) + lop_doubles(n, kTileStages) +
                            rfl_doubles(n, kTileStages) + rinfo_doubles(n, kTileStages)) +
          sizeof(int4) * kTileStages;
+}
+
+// resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved per
+// block) and the launch bounds' register budget (general 3, periodic 4)
+int tile_blocks_per_sm(int n, int chunk, bool periodic_step)
+{
+  const int K = tile_instance_k(chunk);
+  const size_t smem = periodic_step ? sizeof(double) * kTileStages * tile_stage_doubles(n, K) +
+                                          (sizeof(PMeta) + sizeof(int4)) * kTileStages
+                                    : tile_smem_bytes(n, chunk);
+  int fit = (int)((228 * 1024) / (smem + 1024));
+  const int regs_fit = periodic_step ? 4 : 3;
+  return fit < 1 ? 1 : fit > regs_fit ? regs_fit : fit;
 }
 
 template <int N, int K>
