@@ -80,9 +80,9 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_share.argtypes = [vp, c_int, vp]
     L.faces_batch_share_n.argtypes = [vp, c_int, c_int, vp]
     L.faces_batch_share_each.argtypes = [vp, c_int, vp]
-    L.faces_batch_tune.argtypes = [vp, c_int, c_int]
+    L.faces_batch_tune.argtypes = [vp, c_int, c_int, c_int]
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
-    L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip]
+    L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
     jp, sp = ctypes.POINTER(FacesJob), ctypes.POINTER(ServeStats)
     llp, dblp = ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)
@@ -353,8 +353,8 @@ class Batch:
     def share_each(self, compute: bool = True, stream=None) -> None:
         _check(lib().faces_batch_share_each(self._h, int(compute), _stream(stream)))
 
-    def tune(self, unit_div: int = 0, blocks_per_sm: int = 0) -> None:
-        _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm))
+    def tune(self, unit_div: int = 0, blocks_per_sm: int = 0, half: int = -1) -> None:
+        _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm, half))
 
     def autotune(self, trials: int = 3, stream=None) -> int:
         """Keeps the fastest work split; returns the shares it applied to
@@ -362,9 +362,9 @@ class Batch:
         return _check(lib().faces_batch_autotune(self._h, trials, _stream(stream)))
 
     def info(self) -> dict:
-        v = [ctypes.c_int() for _ in range(5)]
+        v = [ctypes.c_int() for _ in range(6)]
         _check(lib().faces_batch_info(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks"), (x.value for x in v)))
+        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks", "half"), (x.value for x in v)))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

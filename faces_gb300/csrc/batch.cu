@@ -38,27 +38,30 @@ using namespace tiledev;
 namespace {
 
 // elements per tile for each n: as many as fit a ~20 KB stage, a power of 2
-__host__ __device__ constexpr int bk(int n) { return tile_kmax(n); }
+// (h = 1: half as many, so that stages are small enough for 4 resident
+// blocks per SM)
+__host__ __device__ constexpr int bk(int n, int h) { return h && tile_kmax(n) > 1 ? tile_kmax(n) / 2 : tile_kmax(n); }
 __host__ __device__ constexpr int bspt(int n) { return (n * n * pieces_per_row(n) + 255) / 256; }
 
 constexpr int kBatchStages = 3;
 constexpr int kNNMax = kBatchMaxN * kBatchMaxN;
 
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
-__host__ __device__ constexpr int stage_of(int n) { return bk(n) * n * n * smem_row_stride(n) + 2 * n * n; }
-__host__ __device__ constexpr int stage_max(int n)
+__host__ __device__ constexpr int stage_of(int n, int h) { return bk(n, h) * n * n * smem_row_stride(n) + 2 * n * n; }
+__host__ __device__ constexpr int stage_max(int n, int h)
 {
-  return n < kBatchMinN ? 0 : cmax(stage_of(n), stage_max(n - 1));
+  return n < kBatchMinN ? 0 : cmax(stage_of(n, h), stage_max(n - 1, h));
 }
 __host__ __device__ constexpr int spt_max(int n) { return n < kBatchMinN ? 0 : cmax(bspt(n), spt_max(n - 1)); }
 
-constexpr int kStage = (stage_max(kBatchMaxN) + 1) & ~1;
+template <int H>
+constexpr int kStage = (stage_max(kBatchMaxN, H) + 1) & ~1;
 constexpr int kSptMax = spt_max(kBatchMaxN);
 
 // shared memory: data stages, then per-stage row arrays sized for n = 10
-constexpr long batch_smem_bytes()
+constexpr long batch_smem_bytes(int h)
 {
-  return sizeof(double) * (long)kBatchStages * kStage + sizeof(double *) * (long)kBatchStages * kNNMax +
+  return sizeof(double) * (long)kBatchStages * (h ? kStage<1> : kStage<0>) + sizeof(double *) * (long)kBatchStages * kNNMax +
          sizeof(SlotCol) * (long)kBatchStages * kNNMax + sizeof(unsigned) * (long)kBatchStages * kNNMax +
          sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages;
 }
@@ -103,13 +106,14 @@ struct Smem {
   PMeta *meta;
 };
 
+template <int H>
 __device__ __forceinline__ Smem smem_layout(double *sm)
 {
-  static_assert(kStage % 2 == 0, "stages keep 16-byte alignment");
+  static_assert(kStage<H> % 2 == 0, "stages keep 16-byte alignment");
   static_assert((kBatchStages * kNNMax * sizeof(unsigned)) % 16 == 0, "tile infos stay 16-byte aligned");
   Smem m;
   m.data = sm;
-  m.lop = reinterpret_cast<double **>(sm + (long)kBatchStages * kStage);
+  m.lop = reinterpret_cast<double **>(sm + (long)kBatchStages * kStage<H>);
   m.rinfo = reinterpret_cast<SlotCol *>(m.lop + kBatchStages * kNNMax);
   m.rfl = reinterpret_cast<unsigned *>(m.rinfo + kBatchStages * kNNMax);
   m.tinfo = reinterpret_cast<int4 *>(m.rfl + kBatchStages * kNNMax);
@@ -119,27 +123,27 @@ __device__ __forceinline__ Smem smem_layout(double *sm)
 
 // MODE: 0 every field takes the general step, 1 every field the periodic
 // step, 2 each field its own
-template <int N, int MODE>
+template <int N, int MODE, int H>
 __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u, ColKey &ck, bool &have_col,
                                        SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
   if (MODE == 1 || (MODE == 2 && bf.lean))
-    ptile::pstage<N, bk(N)>(bf.f, bf.p, u, m.data + (long)st * kStage, m.meta + st, m.tinfo + st);
+    ptile::pstage<N, bk(N, H)>(bf.f, bf.p, u, m.data + (long)st * kStage<H>, m.meta + st, m.tinfo + st);
   else
-    stage_tile<N, bk(N), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage,
+    stage_tile<N, bk(N, H), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage<H>,
                                   m.rfl + st * kNNMax, m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
 }
 
 // stage tile u of field `field` into stage st; the tile info's z holds
 // hi_x | lean << 1 | n << 2 and w the field
-template <int MODE>
+template <int MODE, int H>
 __device__ __forceinline__ void bstage_any(const BatchField *fields, int field, const TileCursor &u, ColKey &ck,
                                            bool &have_col, SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
   const BatchField &bf = fields[field];
   switch (bf.f.n) {
 #define FACES_BSTAGE(NV) \
-  case NV: bstage<NV, MODE>(bf, u, ck, have_col, col, m, st); break;
+  case NV: bstage<NV, MODE, H>(bf, u, ck, have_col, col, m, st); break;
     FACES_BSTAGE(2) FACES_BSTAGE(3) FACES_BSTAGE(4) FACES_BSTAGE(5) FACES_BSTAGE(6) FACES_BSTAGE(7) FACES_BSTAGE(8)
     FACES_BSTAGE(9) FACES_BSTAGE(10)
 #undef FACES_BSTAGE
@@ -156,11 +160,12 @@ __device__ __forceinline__ void bstage_any(const BatchField *fields, int field, 
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits)
+template <int MODE, int H>
+__global__ void __launch_bounds__(256, H ? 4 : 3)
+    batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits)
 {
   extern __shared__ __align__(16) double sm[];
-  const Smem m = smem_layout(sm);
+  const Smem m = smem_layout<H>(sm);
   BWalk nw;  // next tile to stage
   nw.u = blockIdx.x;
   nw.done = nw.u >= nunits;
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
   for (int j = 0; j < kBatchStages - 1; j++) {
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any<MODE>(fields, nw.field, nw.cur, ck, have_col, col, m, j);
+      bstage_any<MODE, H>(fields, nw.field, nw.cur, ck, have_col, col, m, j);
       bwalk_next(fields, units, nunits, nw);
       inflight++;
     } else {
@@ -196,21 +201,21 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
     const int sn = (s + kBatchStages - 1) % kBatchStages;
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any<MODE>(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
+      bstage_any<MODE, H>(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
       bwalk_next(fields, units, nunits, nw);
       inflight++;
     } else {
       cp_commit();
     }
-    double *buf = m.data + (long)s * kStage;
+    double *buf = m.data + (long)s * kStage<H>;
     // periodic step: x pairs, barrier, y/z pairs (each storing its finals);
     // general step: sums (with their own barriers), barrier, store
     if (nk > 0) {
       switch (n) {
 #define FACES_BSUM(NV)                                                       \
   case NV:                                                                   \
-    if (lean) ptile::pxpass<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk); \
-    else sum_tile<NV, bk(NV)>(buf, rfl, nk, hx, regular != 0);               \
+    if (lean) ptile::pxpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk); \
+    else sum_tile<NV, bk(NV, H)>(buf, rfl, nk, hx, regular != 0);               \
     break;
         FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
         FACES_BSUM(9) FACES_BSUM(10)
@@ -224,9 +229,9 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
 #define FACES_BSTORE(NV)                                                                                  \
   case NV:                                                                                                 \
     if (lean)                                                                                              \
-      ptile::pyzpass<NV, bk(NV)>(fields[ti.w].f, buf, m.meta + s, nk);                                     \
+      ptile::pyzpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk);                                  \
     else                                                                                                   \
-      store_tile<NV, bk(NV), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
+      store_tile<NV, bk(NV, H), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;
         FACES_BSTORE(2) FACES_BSTORE(3) FACES_BSTORE(4) FACES_BSTORE(5) FACES_BSTORE(6) FACES_BSTORE(7)
         FACES_BSTORE(8) FACES_BSTORE(9) FACES_BSTORE(10)
@@ -240,22 +245,26 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchField *fields,
 
 }  // namespace
 
-RowPlan batch_plan(const FieldDesc &f)
+RowPlan batch_plan(const FieldDesc &f, int half)
 {
-  RowPlan p = make_row_plan(f, batch_n_supported(f.n) ? bk(f.n) : 1, 0);
+  RowPlan p = make_row_plan(f, batch_n_supported(f.n) ? bk(f.n, half) : 1, 0);
   p.order = 2;
   p.unit_chunks = 1;
   return p;
 }
 
-int batch_blocks_per_sm() { return std::max(1, std::min(3, (int)((228 * 1024) / (batch_smem_bytes() + 1024)))); }
+int batch_blocks_per_sm(int half)
+{
+  return std::max(1, std::min(half ? 4 : 3, (int)((228 * 1024) / (batch_smem_bytes(half) + 1024))));
+}
 
 cudaError_t batch_configure()
 {
-  const int smem = (int)batch_smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(batch_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int s0 = (int)batch_smem_bytes(0), s1 = (int)batch_smem_bytes(1);
+  cudaError_t e = cudaFuncSetAttribute(batch_kernel<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, s0);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, s0);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, s0);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1);
   return e;
 }
 
@@ -275,13 +284,15 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
 }
 
 cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
-                         cudaStream_t s)
+                         int half, cudaStream_t s)
 {
   if (nunits <= 0 || grid <= 0) return cudaSuccess;
-  const size_t smem = batch_smem_bytes();
-  if (mode == 1) batch_kernel<1><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
-  else if (mode == 2) batch_kernel<2><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
-  else batch_kernel<0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  if (half && mode != 1) return cudaErrorInvalidValue;  // half-length tiles: periodic step only
+  const size_t smem = batch_smem_bytes(half);
+  if (mode == 1 && half) batch_kernel<1, 1><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  else if (mode == 1) batch_kernel<1, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  else if (mode == 2) batch_kernel<2, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  else batch_kernel<0, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
   return cudaGetLastError();
 }
 
@@ -320,6 +331,7 @@ struct faces_batch {
   BatchUnit *d_units = nullptr;
   int nunits = 0;
   int mode = 0;      // batch_mode of the fused fields
+  int half = 0;      // half-length tiles (mode 1 only), 4 blocks per SM
   int unit_div = 2;  // units are 1/unit_div of a column's chunks
   int per_sm = 3;
   int sms = 0;
@@ -366,14 +378,27 @@ int build_units(faces_batch *b)
     CUDA_TRY(cudaMemcpy(b->d_units, units.data(), sizeof(BatchUnit) * units.size(), cudaMemcpyHostToDevice),
              "faces_batch: work list upload");
   }
-  b->grid = std::min<long>((long)b->sms * b->per_sm, std::max(1, b->nunits));
+  if (b->mode != 1 && b->half) return fail(FACES_EINVAL, "faces_batch: half-length tiles need all fields periodic");
+  b->grid = std::min<long>((long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half)), std::max(1, b->nunits));
   drop_graphs(b);
+  return FACES_OK;
+}
+
+// tile plans of every field for full (0) or half-length (1) tiles
+int set_half(faces_batch *b, int half)
+{
+  b->half = half;
+  for (size_t i = 0; i < b->h_fields.size(); i++) b->h_fields[i].p = batch_plan(b->h_fields[i].f, half);
+  if (!b->h_fields.empty())
+    CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * b->h_fields.size(),
+                        cudaMemcpyHostToDevice),
+             "faces_batch: field table upload");
   return FACES_OK;
 }
 
 int launch_batched(faces_batch *b, cudaStream_t s)
 {
-  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->mode, s), "batch kernel launch");
+  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->mode, b->half, s), "batch kernel launch");
   return FACES_OK;
 }
 
@@ -437,7 +462,7 @@ int faces_batch_commit(faces_batch *b)
     const faces_ctx *c = b->ctx[i];
     BatchField bf;
     bf.f = c->desc(b->u[i]);
-    bf.p = batch_plan(bf.f);
+    bf.p = batch_plan(bf.f, 0);
     bf.lean = ptile_field(bf.f) && !(c->flags & FACES_GENERAL);
     b->h_fields[i] = bf;
     b->fused[i] = batch_eligible(c) ? 1 : 0;
@@ -448,7 +473,7 @@ int faces_batch_commit(faces_batch *b)
              "faces_batch: field table upload");
   }
   CUDA_TRY(batch_configure(), "faces_batch: shared memory attribute");
-  b->per_sm = batch_blocks_per_sm();
+  b->per_sm = batch_blocks_per_sm(0);
   CUDA_TRY(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "faces_batch: capture stream");
   b->committed = true;
   return build_units(b);
@@ -499,11 +524,14 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream)
   return share_others(b, compute, true, stream);
 }
 
-int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm)
+int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half)
 {
   if (int rc = check_batch(b, true)) return rc;
+  if (half > 0 && b->mode != 1) return fail(FACES_EINVAL, "half-length tiles need every batched field periodic");
+  if (half >= 0 && half != b->half)
+    if (int rc = set_half(b, half ? 1 : 0)) return rc;
   if (unit_div > 0) b->unit_div = unit_div;
-  if (blocks_per_sm > 0) b->per_sm = std::min(blocks_per_sm, batch_blocks_per_sm());
+  if (blocks_per_sm > 0) b->per_sm = blocks_per_sm;
   return build_units(b);
 }
 
@@ -512,45 +540,60 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
   if (int rc = check_batch(b, true)) return rc;
   if (trials < 1) trials = 3;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int fit = batch_blocks_per_sm();
+  // candidates: tile length (full, or half when every field is periodic),
+  // units per column, resident blocks per SM (the most that fit, one fewer)
+  struct Cand {
+    int half, div, per_sm;
+  };
+  std::vector<Cand> cands;
+  const int divs[] = {1, 2, 4, 8, 64};
+  for (int h = 0; h < (b->mode == 1 ? 2 : 1); h++)
+    for (int d : divs)
+      for (int sm = batch_blocks_per_sm(h); sm >= std::max(1, batch_blocks_per_sm(h) - 1); sm--)
+        cands.push_back({h, d, sm});
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
   CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
   float best = 1e30f;
-  int best_div = b->unit_div, best_sm = b->per_sm;
+  Cand pick{b->half, b->unit_div, b->per_sm};
   int applied = 0;  // shares the timed launches applied to each batched field
   int rc = FACES_OK;
-  const int divs[] = {1, 2, 4, 8, 64};
-  for (int d : divs) {
-    for (int sm = fit; sm >= std::max(1, fit - 1) && rc == FACES_OK; sm--) {
-      b->unit_div = d;
-      b->per_sm = sm;
-      if ((rc = build_units(b))) break;
-      if (b->nunits == 0) break;
-      if ((rc = launch_batched(b, s))) break;  // warm-up
-      cudaEventRecord(e0, s);
-      for (int t = 0; t < trials && rc == FACES_OK; t++) rc = launch_batched(b, s);
-      cudaEventRecord(e1, s);
-      applied += 1 + trials;
-      cudaError_t e = cudaEventSynchronize(e1);
-      if (rc == FACES_OK && e != cudaSuccess)
-        rc = fail(FACES_ECUDA, "autotune: synchronize: %s", cudaGetErrorString(e));
-      float ms = 0;
-      if (rc == FACES_OK) cudaEventElapsedTime(&ms, e0, e1);
-      if (rc == FACES_OK && ms < best) { best = ms; best_div = d; best_sm = sm; }
+  for (const Cand &c : cands) {
+    if (c.half != b->half && (rc = set_half(b, c.half))) break;
+    b->unit_div = c.div;
+    b->per_sm = c.per_sm;
+    if ((rc = build_units(b))) break;
+    if (b->nunits == 0) break;
+    if ((rc = launch_batched(b, s))) break;  // warm-up
+    cudaEventRecord(e0, s);
+    for (int t = 0; t < trials && rc == FACES_OK; t++) rc = launch_batched(b, s);
+    cudaEventRecord(e1, s);
+    applied += 1 + trials;
+    if (rc) break;
+    const cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = fail(FACES_ECUDA, "autotune: synchronize: %s", cudaGetErrorString(e));
+      break;
     }
-    if (rc != FACES_OK || b->nunits == 0) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
-  b->unit_div = best_div;
-  b->per_sm = best_sm;
+  if (pick.half != b->half && (rc = set_half(b, pick.half))) return rc;
+  b->unit_div = pick.div;
+  b->per_sm = pick.per_sm;
   if ((rc = build_units(b))) return rc;
   return applied;
 }
 
-int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks)
+int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks,
+                     int *half)
 {
   if (!b) return fail(FACES_EINVAL, "null batch");
   int fu = 0;
@@ -560,6 +603,7 @@ int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *
   if (units) *units = b->nunits;
   if (unit_div) *unit_div = b->unit_div;
   if (blocks) *blocks = (int)b->grid;
+  if (half) *half = b->half;
   return FACES_OK;
 }
 

@@ -28,11 +28,12 @@ struct BatchUnit {
 // n the batched kernel handles (direct mode only)
 inline bool batch_n_supported(int n) { return n >= kBatchMinN && n <= kBatchMaxN; }
 
-// the tile plan of a field in the batched kernel
-RowPlan batch_plan(const FieldDesc &f);
+// the tile plan of a field in the batched kernel (half = 1: half-length
+// tiles, for the periodic-step form that keeps 4 blocks per SM)
+RowPlan batch_plan(const FieldDesc &f, int half = 0);
 
-// resident blocks per SM the kernel's shared memory allows (at most 3)
-int batch_blocks_per_sm();
+// resident blocks per SM (3, or 4 with half-length tiles)
+int batch_blocks_per_sm(int half = 0);
 
 // sets the kernel's shared-memory attribute on the current device (call once
 // per device before the first launch)
@@ -44,8 +45,9 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
 // the kernel form for a field table: 0 all general, 1 all periodic (lean), 2 mixed
 int batch_mode(const BatchField *fields, size_t n);
 
-// one share of every field the units cover; grid blocks stride over the units
+// one share of every field the units cover; grid blocks stride over the
+// units; half = 1 only with mode 1 and plans from batch_plan(f, 1)
 cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
-                         cudaStream_t s);
+                         int half, cudaStream_t s);
 
 }  // namespace faces

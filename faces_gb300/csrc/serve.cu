@@ -208,7 +208,7 @@ int admit(faces_server *s, Job &job)
   f.msg = nullptr;
   f.msg_off = nullptr;
   f.nbr = nbr;
-  job.p = batch_plan(f);
+  job.p = batch_plan(f, 0);
   plain_plan(s, job);
   cudaError_t e;
   if (j.init == 0) e = launch_init_ref(f, s->stream);
@@ -339,7 +339,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          s->kmode, s->stream),
+                          s->kmode, 0, s->stream),
              "server: batched launch");
     s->launches++;
   }
@@ -453,7 +453,7 @@ int faces_server_create(faces_server **out, size_t budget_bytes, int max_jobs, u
     return fail(FACES_ECUDA, "faces_server_create: %s", cudaGetErrorString(e));
   }
   s->base_host = host_seconds();
-  s->per_sm = batch_blocks_per_sm();
+  s->per_sm = batch_blocks_per_sm(0);
   *out = s;
   return FACES_OK;
 }

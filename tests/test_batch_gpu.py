@@ -148,9 +148,11 @@ def test_many_fields(faces_lib):
     assert not bad, [mix[i] for i in bad[:5]]
 
 
-def test_all_periodic_batch_equals_general_step(faces_lib):
+@pytest.mark.parametrize("half", [0, 1], ids=["full_tiles", "half_tiles"])
+def test_all_periodic_batch_equals_general_step(faces_lib, half):
     """A batch of periodic direct-mode fields runs the periodic tile step
-    only; it must equal the general tile step of each field alone."""
+    only (full or half-length tiles); it must equal the general tile step of
+    each field alone."""
     F = faces_lib
     rng = np.random.default_rng(11)
     mix = []
@@ -158,8 +160,8 @@ def test_all_periodic_batch_equals_general_step(faces_lib):
         L = tuple(int(x) for x in rng.integers(1, 3, size=3))
         m = tuple(int(x) for x in rng.integers(1, 9, size=3))
         mix.append((L + m + (int(rng.integers(2, 11)),), True, False))
-    got, info = batched(F, mix, 3, "graph", seed0=500)
-    assert info["fused_fields"] == len(mix)
+    got, info = batched(F, mix, 3, "graph", seed0=500, tune=(0, 0, half))
+    assert info["fused_fields"] == len(mix) and info["half"] == half
     for i, ((shape, _, _), out) in enumerate(zip(mix, got)):
         f = F.Faces(*shape, periodic=True, general=True)
         u = f.field()
@@ -167,4 +169,18 @@ def test_all_periodic_batch_equals_general_step(faces_lib):
         f.share_n(u, 3)
         torch.cuda.synchronize()
         assert np.array_equal(u.cpu().numpy(), out), f"field {i} {shape}"
+        f.close()
+
+
+def test_half_tiles_need_periodic_fields(faces_lib):
+    F = faces_lib
+    fields = make_fields(F, MIX[:4], 1)
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    with pytest.raises(F.FacesError):
+        b.tune(0, 0, 1)
+    b.close()
+    for f, _ in fields:
         f.close()
