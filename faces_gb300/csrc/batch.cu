@@ -128,7 +128,8 @@ __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u
                                        SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
   if (MODE == 1 || (MODE == 2 && bf.lean))
-    ptile::pstage<N, bk(N, H)>(bf.f, bf.p, u, m.data + (long)st * kStage<H>, m.meta + st, m.tinfo + st);
+    ptile::pstage<N, bk(N, H)>(bf.f, bf.p, u, m.data + (long)st * kStage<H>, m.meta + st, m.tinfo + st,
+                               threadIdx.x);
   else
     stage_tile<N, bk(N, H), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage<H>,
                                   m.rfl + st * kNNMax, m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(256, H ? 4 : 3)
       switch (n) {
 #define FACES_BSUM(NV)                                                       \
   case NV:                                                                   \
-    if (lean) ptile::pxpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk); \
+    if (lean) ptile::pxpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk, threadIdx.x); \
     else sum_tile<NV, bk(NV, H)>(buf, rfl, nk, hx, regular != 0);               \
     break;
         FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(256, H ? 4 : 3)
 #define FACES_BSTORE(NV)                                                                                  \
   case NV:                                                                                                 \
     if (lean)                                                                                              \
-      ptile::pyzpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk);                                  \
+      ptile::pyzpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk, threadIdx.x);                     \
     else                                                                                                   \
       store_tile<NV, bk(NV, H), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;

@@ -87,7 +87,9 @@ void replan(faces_ctx &c)
     k = k2;
     while (k > 1 && tile_smem_bytes(c.n, k) > 110 * 1024) k /= 2;
     c.tplan = make_row_plan(f, k, 0);
-    c.tplan.order = c.order >= 0 ? (c.order % 16) : 2;
+    // order 3 (warp tiles) applies to the periodic step only; elsewhere it
+    // means the default
+    c.tplan.order = c.order >= 0 && c.order % 16 != 3 ? (c.order % 16) : 2;
     // order 2 units: chunks per unit (tuning value order = 2 + 16*u), default
     // half a column
     const int uc = c.order >= 16 ? c.order / 16 : (c.tplan.nchunks + 1) / 2;
@@ -98,6 +100,14 @@ void replan(faces_ctx &c)
     const int fit = tile_blocks_per_sm(c.n, k, periodic_step);
     const int per_sm = c.tpb > 0 ? (c.tpb < fit ? c.tpb : fit) : fit;
     c.tgrid = (long)c.sms * (per_sm < 1 ? 1 : per_sm);
+    if (periodic_step && c.order >= 0 && c.order % 16 == 3) {
+      // warp tiles: one warp per tile of tile_kwarp(n) elements
+      c.tplan = make_row_plan(f, tile_kwarp(c.n), 0);
+      c.tplan.order = 3;
+      c.tplan.unit_chunks = 1;
+      const int wfit = wtile_blocks_per_sm(c.n);
+      c.tgrid = (long)c.sms * (c.tpb > 0 && c.tpb < wfit ? c.tpb : wfit);
+    }
   }
 }
 
@@ -221,7 +231,8 @@ int faces_field_free(double *u)
 int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
 {
   if (int rc = check_ctx(c)) return rc;
-  if (order % 16 > 2) return fail(FACES_EINVAL, "order = %d: -1 (default), 0, 1, or 2 + 16*chunks_per_unit", order);
+  if (order % 16 > 3)
+    return fail(FACES_EINVAL, "order = %d: -1 (default), 0, 1, 2 + 16*chunks_per_unit, or 3 (warp tiles)", order);
   c->chunk = chunk > 0 ? chunk : 0;
   c->tpb = width > 0 ? width : 0;
   c->order = order;
@@ -256,7 +267,10 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   const bool fused = compute && !(c->flags & FACES_GATHER);
   if (fused && !(c->flags & FACES_ROWS) && tile_kernel_supported(c->n))
-    CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, (c->flags & FACES_GENERAL) != 0), "tile kernel launch");
+  {
+    if (c->tplan.order == 3) CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
+    else CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, (c->flags & FACES_GENERAL) != 0), "tile kernel launch");
+  }
   else if (fused && row_kernel_supported(c->n))
     CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
   else
@@ -292,7 +306,7 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   // chunk or half a column (order 2 + 16*u), resident blocks per SM
   const int k0 = c->tplan.chunk;
   const int ks[3] = {k0, k0 / 2, k0 * 2};
-  const int orders[2] = {-1, 2 + 16};
+  const int orders[3] = {-1, 2 + 16, 3};
   const int widths[2] = {0, 2};
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
@@ -304,6 +318,7 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
     for (int o : orders)
       for (int w : widths) {
         if (rc != FACES_OK) break;
+        if (o == 3 && ki > 0) continue;  // warp tiles have one tile length
         c->chunk = ks[ki];
         c->order = o;
         c->tpb = w;

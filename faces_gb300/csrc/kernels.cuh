@@ -26,6 +26,12 @@ bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);
 size_t tile_smem_bytes(int n, int chunk);
 int tile_blocks_per_sm(int n, int chunk, bool periodic_step);
+// the warp-tile form of the periodic step (periodic direct-mode fields; plan
+// chunk at most tile_kwarp(n)); grid in blocks of 4 warps
+size_t wtile_smem_bytes(int n);
+int wtile_blocks_per_sm(int n);
+cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);
+
 // periodic direct-mode fields take the periodic tile step unless `general`
 cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false);
 

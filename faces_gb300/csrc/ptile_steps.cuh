@@ -91,57 +91,57 @@ __device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, int &pc)
   }
 }
 
-// Threads and needed slots: with more than 128 slots per element thread t
-// takes slots t, t+256, ... (SPT of them) for every element of the tile;
-// with fewer, KT = 256/slots threads share a slot and thread t takes its
-// elements t/slots, +KT, ...  A thread decodes its slot once per tile and
-// walks the elements by adding the element stride.
-template <int N>
+// A team of T threads (a block of 256, or one warp) works on a tile; t is
+// the thread's index in its team.  Threads and needed slots: with more than
+// T/2 slots per element thread t takes slots t, t+T, ... (SPT of them) for
+// every element of the tile; with fewer, KT = T/slots threads share a slot
+// and thread t takes its elements t/slots, +KT, ...  A thread decodes its
+// slot once per tile and walks the elements by adding the element stride.
+template <int N, int T>
 struct PSlots {
   static constexpr int NE = Needed<N>::count;
-  static constexpr int KT = NE <= 128 ? 256 / NE : 1;
-  static constexpr int SPT = KT > 1 ? 1 : (NE + 255) / 256;
+  static constexpr int KT = NE <= T / 2 ? T / NE : 1;
+  static constexpr int SPT = KT > 1 ? 1 : (NE + T - 1) / T;
 };
 
-template <int N>
-__device__ __forceinline__ bool pslot(int jj, int &j, int &kq)
+template <int N, int T>
+__device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
 {
-  constexpr int NE = PSlots<N>::NE, KT = PSlots<N>::KT;
+  constexpr int NE = PSlots<N, T>::NE, KT = PSlots<N, T>::KT;
   if constexpr (KT > 1) {
-    j = (int)threadIdx.x % NE;
-    kq = (int)threadIdx.x / NE;
+    j = t % NE;
+    kq = t / NE;
     return kq < KT;
   } else {
-    j = (int)threadIdx.x + jj * 256;
+    j = t + jj * T;
     kq = 0;
     return j < NE;
   }
 }
 
 // Stage tile u: the needed pieces of its elements, and the x-lower ends.
-template <int N, int K>
+template <int N, int K, int T = 256>
 __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, const TileCursor &u, double *buf,
-                                       PMeta *meta, int4 *tinfo)
+                                       PMeta *meta, int4 *tinfo, int t)
 {
   constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
-  constexpr int KT = PSlots<N>::KT, SPT = PSlots<N>::SPT;
+  constexpr int KT = PSlots<N, T>::KT, SPT = PSlots<N, T>::SPT;
   constexpr long N3 = (long)N * N * N;
   const int jx0 = u.c * p.chunk;
   const int nk = min(p.chunk, f.m[0] - jx0);
   const bool first = u.c == 0;
   const int jxl = first ? f.m[0] - 1 : jx0 - 1;
-  if (threadIdx.x < 4) {
-    const int s = threadIdx.x;
-    meta->off[s] = col_off<N>(f, u, s, false, jx0);
-    meta->lo[s] = col_off<N>(f, u, s, first, jxl);
+  if (t < 4) {
+    meta->off[t] = col_off<N>(f, u, t, false, jx0);
+    meta->lo[t] = col_off<N>(f, u, t, first, jxl);
   }
-  if (threadIdx.x == 0) *tinfo = make_int4(jx0, nk, 0, 0);
+  if (t == 0) *tinfo = make_int4(jx0, nk, 0, 0);
   const long o0 = col_off<N>(f, u, 0, false, jx0), o1 = col_off<N>(f, u, 1, false, jx0);
   const long o2 = col_off<N>(f, u, 2, false, jx0), o3 = col_off<N>(f, u, 3, false, jx0);
 #pragma unroll
   for (int jj = 0; jj < SPT; jj++) {
     int j, kq;
-    if (!pslot<N>(jj, j, kq)) continue;
+    if (!pslot<N, T>(jj, t, j, kq)) continue;
     int sy, sz, pc;
     needed_piece<N>(j, sy, sz, pc);
     const int s = col_sel<N>(sy, sz);
@@ -150,8 +150,8 @@ __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, con
     double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
     for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) cp_async(sp, g, PW);
   }
-  if ((int)threadIdx.x < NN) {
-    const int r = threadIdx.x, sy = r % N, sz = r / N;
+  for (int r = t; r < NN; r += T) {
+    const int sy = r % N, sz = r / N;
     const long ol = col_off<N>(f, u, col_sel<N>(sy, sz), first, jxl);
     cp_async(buf + K * NN * RS + r, f.u + ol + sz * NN + sy * N + (N - 1), 1);
   }
@@ -167,14 +167,14 @@ __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, con
 //              are disjoint, so one phase does them all.
 // The order is the general step's (x, then y, then z pairs) and every stored
 // cell is one the general step stores, without the unchanged ones.
-template <int N, int K>
-__device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PMeta *meta, int nk)
+template <int N, int K, int T = 256>
+__device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
   double *locol = buf + K * NN * RS;
   const int items = nk * NN;
-  for (int i = threadIdx.x; i < items; i += blockDim.x) {
+  for (int i = t; i < items; i += T) {
     const int k = i / NN, r = i - k * NN;
     double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (N - 1);
     double *hi = buf + (k * NN + r) * RS;
@@ -192,15 +192,15 @@ __device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PM
   }
 }
 
-template <int N, int K>
-__device__ __forceinline__ void pyzpass(const FieldDesc &f, const double *buf, const PMeta *meta, int nk)
+template <int N, int K, int T = 256>
+__device__ __forceinline__ void pyzpass(const FieldDesc &f, const double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
   constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
   const double *locol = buf + K * NN * RS;
   const int last_c = (nk - 1) * N + (N - 1);  // the next chunk's seam: not stored
-  for (int i = threadIdx.x; i < G * COLS; i += blockDim.x) {
+  for (int i = t; i < G * COLS; i += T) {
     const int g = i / COLS, c = i - g * COLS;
     const double *sb;
     int srs;

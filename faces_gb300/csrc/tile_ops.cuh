@@ -334,6 +334,18 @@ FACES_HD constexpr int tile_kmax(int n)
                                                            : 1;
 }
 
+// Elements per tile of the warp-tile form (one warp per tile): as many as
+// fit a ~6 KB stage, a power of 2 in [1, 32].
+FACES_HD constexpr int tile_kwarp(int n)
+{
+  return 6144 / (n * n * smem_row_stride(n) * 8) >= 32 ? 32
+         : 6144 / (n * n * smem_row_stride(n) * 8) >= 16 ? 16
+         : 6144 / (n * n * smem_row_stride(n) * 8) >= 8  ? 8
+         : 6144 / (n * n * smem_row_stride(n) * 8) >= 4  ? 4
+         : 6144 / (n * n * smem_row_stride(n) * 8) >= 2  ? 2
+                                                          : 1;
+}
+
 // the kernel is instantiated for K = 1, 2, 4, ..., tile_kinst_max(n)
 // elements per tile; a plan whose chunk is smaller (clamped to mx) runs in
 // the next larger instance

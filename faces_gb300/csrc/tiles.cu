@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
 #pragma unroll
   for (int j = 0; j < NS - 1; j++) {
     if (!nw.done) {
-      ptile::pstage<N, K>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j);
+      ptile::pstage<N, K>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j, threadIdx.x);
       walk_next(p, nw);
       inflight++;
     } else {
@@ -119,17 +119,136 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
     const int nk = tinfo[s].y;
     const int sn = (s + NS - 1) % NS;
     if (!nw.done) {
-      ptile::pstage<N, K>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn);
+      ptile::pstage<N, K>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn, threadIdx.x);
       walk_next(p, nw);
       inflight++;
     } else {
       cp_commit();
     }
     double *buf = sm + s * stage;
-    ptile::pxpass<N, K>(f, buf, meta + s, nk);
+    ptile::pxpass<N, K>(f, buf, meta + s, nk, threadIdx.x);
     __syncthreads();
-    ptile::pyzpass<N, K>(f, buf, meta + s, nk);
+    ptile::pyzpass<N, K>(f, buf, meta + s, nk, threadIdx.x);
     s = (s + 1) % NS;
+  }
+}
+
+// The warp-tile form of the periodic step: every warp stages, sums and
+// stores its own tiles (tile_kwarp(n) elements, kWarpStages stages), so a
+// block holds kWarpsPerBlock independent pipelines and needs no block
+// barrier; warps walk the tiles chunk group first (tile q: chunk q / columns,
+// column q % columns) with a stride of all warps of the grid.
+constexpr int kWarpsPerBlock = 4;
+// stages per warp: 3 where a stage is at most 8 KB, else 2 (so that blocks of
+// large n still fit several to an SM)
+__host__ __device__ constexpr int wtile_stages(int n)
+{
+  return (tile_kwarp(n) * n * n * smem_row_stride(n) + 2 * n * n) * 8 <= 8192 ? 3 : 2;
+}
+
+template <int N, int K, int NS, int WPB>
+__global__ void __launch_bounds__(WPB * 32) wtile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *wsm = sm + (long)warp * NS * stage;
+  PMeta *meta_all = reinterpret_cast<PMeta *>(sm + (long)WPB * NS * stage);
+  PMeta *meta = meta_all + warp * NS;
+  int4 *tinfo = reinterpret_cast<int4 *>(meta_all + WPB * NS) + warp * NS;
+  const int ncol = (int)(p.ntiles / p.nchunks), total = (int)p.ntiles;
+  const int stride = gridDim.x * WPB;
+  int q = blockIdx.x * WPB + warp;  // next tile to stage
+  auto cursor = [&](int t) {
+    TileCursor u;
+    u.c = t / ncol;
+    const int col = t - u.c * ncol, t2 = col / p.ty;
+    u.jy = col - t2 * p.ty;
+    u.jz = t2 % p.tz;
+    u.r = t2 / p.tz;
+    return u;
+  };
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (q < total) {
+      ptile::pstage<N, K, 32>(f, p, cursor(q), wsm + j * stage, meta + j, tinfo + j, lane);
+      q += stride;
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    // the staged tile and its infos, and the end of the previous tile's work
+    __syncwarp();
+    const int nk = tinfo[s].y;
+    const int sn = (s + NS - 1) % NS;
+    if (q < total) {
+      ptile::pstage<N, K, 32>(f, p, cursor(q), wsm + sn * stage, meta + sn, tinfo + sn, lane);
+      q += stride;
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = wsm + s * stage;
+    ptile::pxpass<N, K, 32>(f, buf, meta + s, nk, lane);
+    __syncwarp();
+    ptile::pyzpass<N, K, 32>(f, buf, meta + s, nk, lane);
+    s = (s + 1) % NS;
+  }
+}
+
+size_t wtile_smem_bytes(int n)
+{
+  return sizeof(double) * kWarpsPerBlock * wtile_stages(n) * tile_stage_doubles(n, tile_kwarp(n)) +
+         (sizeof(PMeta) + sizeof(int4)) * kWarpsPerBlock * wtile_stages(n);
+}
+
+int wtile_blocks_per_sm(int n)
+{
+  const int fit = (int)((228 * 1024) / (wtile_smem_bytes(n) + 1024));
+  return fit < 1 ? 1 : fit > 16 ? 16 : fit;
+}
+
+template <int N>
+static cudaError_t launch_wtiles_n(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+{
+  constexpr int K = tile_kwarp(N);
+  if (p.chunk > K) return cudaErrorInvalidValue;
+  const size_t smem = wtile_smem_bytes(N);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  long blocks = (p.ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (grid < blocks) blocks = grid;
+  if (blocks < 1) return cudaSuccess;
+  wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock><<<(unsigned)blocks, 32 * kWarpsPerBlock, smem, s>>>(f, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+{
+  if (!ptile_field(f)) return cudaErrorInvalidValue;
+  switch (f.n) {
+    case 2: return launch_wtiles_n<2>(f, p, grid, s);
+    case 3: return launch_wtiles_n<3>(f, p, grid, s);
+    case 4: return launch_wtiles_n<4>(f, p, grid, s);
+    case 5: return launch_wtiles_n<5>(f, p, grid, s);
+    case 6: return launch_wtiles_n<6>(f, p, grid, s);
+    case 7: return launch_wtiles_n<7>(f, p, grid, s);
+    case 8: return launch_wtiles_n<8>(f, p, grid, s);
+    case 9: return launch_wtiles_n<9>(f, p, grid, s);
+    case 10: return launch_wtiles_n<10>(f, p, grid, s);
+    case 11: return launch_wtiles_n<11>(f, p, grid, s);
+    case 12: return launch_wtiles_n<12>(f, p, grid, s);
+    default: return cudaErrorInvalidValue;
   }
 }
 

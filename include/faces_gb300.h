@@ -122,8 +122,9 @@ int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int comput
  * block for the row kernel, resident blocks per SM for the tile kernel, and
  * the tile kernel's order (< 0: default = 2, 0: blocks stride over the tiles,
  * 1: each block takes a contiguous range of x-chunks, 2 + 16*u: blocks stride
- * over units of u consecutive x-chunks of a column, listed chunk group first;
- * u = 0: one chunk for the periodic step, half a column otherwise). */
+ * over units of u consecutive x-chunks of a column, listed chunk group first,
+ * u = 0 half a column; 3: periodic step only, one warp per tile instead of
+ * one block, no block barriers). */
 int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 
 /* Times the tile step on the field u over elements per tile (default, half,

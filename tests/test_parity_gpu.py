@@ -185,3 +185,25 @@ def test_v6_bit_exact(oracle, faces_lib, shape, periodic):
             if init == "int":
                 assert np.array_equal(out, O.groups_share(s, ref0.copy(), compute, 3))
             assert chk.passed, (init, compute, chk.maxrel)
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1, 4, 4, 4, 5), (1, 1, 1, 3, 2, 5, 8), (3, 3, 3, 2, 2, 2, 6),
+                                   (2, 2, 2, 1, 1, 1, 7), (1, 1, 1, 5, 2, 3, 10), (1, 3, 1, 3, 1, 2, 9),
+                                   (2, 1, 2, 2, 2, 1, 12), (1, 1, 1, 9, 3, 2, 2), (1, 1, 1, 33, 2, 3, 3),
+                                   (2, 1, 1, 7, 3, 2, 4)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_warp_tiles_bit_exact(oracle, faces_lib, shape):
+    """Tile order 3: the periodic step with one warp per tile."""
+    O, F = oracle, faces_lib
+    s = O.Shape(*shape, periodic=True)
+    for init in ("int", "ref"):
+        f = F.Faces(*shape, periodic=True)
+        f.set_tuning(order=3)
+        u = f.field()
+        f.init_int(u, 5) if init == "int" else f.init_ref(u)
+        f.share_n(u, 3)
+        torch.cuda.synchronize()
+        out = u.cpu().numpy()
+        f.close()
+        ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
+        assert np.array_equal(out, O.groups_share(s, ref0, True, 3)), init
