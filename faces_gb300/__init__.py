@@ -82,7 +82,7 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_share_each.argtypes = [vp, c_int, vp]
     L.faces_batch_tune.argtypes = [vp, c_int, c_int, c_int]
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
-    L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip]
+    L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
     jp, sp = ctypes.POINTER(FacesJob), ctypes.POINTER(ServeStats)
     llp, dblp = ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)
@@ -362,9 +362,10 @@ class Batch:
         return _check(lib().faces_batch_autotune(self._h, trials, _stream(stream)))
 
     def info(self) -> dict:
-        v = [ctypes.c_int() for _ in range(6)]
+        v = [ctypes.c_int() for _ in range(7)]
         _check(lib().faces_batch_info(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks", "half"), (x.value for x in v)))
+        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks", "half", "run"),
+                        (x.value for x in v)))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -39,8 +39,15 @@ namespace {
 
 // elements per tile for each n: as many as fit a ~20 KB stage, a power of 2
 // (h = 1: half as many, so that stages are small enough for 4 resident
-// blocks per SM)
-__host__ __device__ constexpr int bk(int n, int h) { return h && tile_kmax(n) > 1 ? tile_kmax(n) / 2 : tile_kmax(n); }
+// blocks per SM; h = 2: as many as fit ~28 KB, 2 resident blocks per SM)
+__host__ __device__ constexpr int pow2_floor(int k) { return k >= 32 ? 32 : k >= 16 ? 16 : k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1; }
+__host__ __device__ constexpr int bk(int n, int h)
+{
+  return h == 2 ? pow2_floor(28672 / (n * n * smem_row_stride(n) * 8))
+         : h == 1 && tile_kmax(n) > 1 ? tile_kmax(n) / 2
+                                       : tile_kmax(n);
+}
+__host__ __device__ constexpr int bblocks(int h) { return h == 2 ? 2 : h == 1 ? 4 : 3; }
 __host__ __device__ constexpr int bspt(int n) { return (n * n * pieces_per_row(n) + 255) / 256; }
 
 constexpr int kBatchStages = 3;
@@ -61,13 +68,13 @@ constexpr int kSptMax = spt_max(kBatchMaxN);
 // shared memory: data stages, then per-stage row arrays sized for n = 10
 constexpr long batch_smem_bytes(int h)
 {
-  return sizeof(double) * (long)kBatchStages * (h ? kStage<1> : kStage<0>) + sizeof(double *) * (long)kBatchStages * kNNMax +
+  return sizeof(double) * (long)kBatchStages * (h == 2 ? kStage<2> : h ? kStage<1> : kStage<0>) + sizeof(double *) * (long)kBatchStages * kNNMax +
          sizeof(SlotCol) * (long)kBatchStages * kNNMax + sizeof(unsigned) * (long)kBatchStages * kNNMax +
-         sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages;
+         sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages + sizeof(BatchField);
 }
 
 struct BWalk {
-  int u, c, c1, field;
+  int u, u_end, run_index, c, c1, field;  // unit, end and index of the current run of units
   TileCursor cur;
   bool done;
 };
@@ -82,17 +89,32 @@ __device__ __forceinline__ void bwalk_unit(const BatchField *fields, const Batch
   w.cur = cursor_of(p, (long)un.column * p.nchunks + un.c0);
 }
 
-__device__ __forceinline__ void bwalk_next(const BatchField *fields, const BatchUnit *units, int nunits, BWalk &w)
+// Blocks take runs of `run` consecutive units: block b the runs b, b + grid,
+// b + 2 grid, ...  Consecutive tiles of a block then mostly belong to one
+// field (its description stays in shared memory), and the blocks running at
+// one time cover a narrow window of the work list (fields in order of n: one
+// n's code).
+__device__ __forceinline__ bool bwalk_run(int run, int nunits, int r, BWalk &w)
+{
+  w.run_index = r;
+  w.u = r * run;
+  w.u_end = min(w.u + run, nunits);
+  return w.u < nunits;
+}
+
+__device__ __forceinline__ void bwalk_next(const BatchField *fields, const BatchUnit *units, int nunits, int run,
+                                           BWalk &w)
 {
   if (w.c + 1 < w.c1) {
     w.c++;
     w.cur.c++;
     return;
   }
-  w.u += gridDim.x;
-  if (w.u >= nunits) {
-    w.done = true;
-    return;
+  if (++w.u >= w.u_end) {
+    if (!bwalk_run(run, nunits, w.run_index + gridDim.x, w)) {
+      w.done = true;
+      return;
+    }
   }
   bwalk_unit(fields, units, w);
 }
@@ -104,6 +126,7 @@ struct Smem {
   unsigned *rfl;
   int4 *tinfo;
   PMeta *meta;
+  BatchField *field;  // the block's copy of the field it stages
 };
 
 template <int H>
@@ -118,6 +141,7 @@ __device__ __forceinline__ Smem smem_layout(double *sm)
   m.rfl = reinterpret_cast<unsigned *>(m.rinfo + kBatchStages * kNNMax);
   m.tinfo = reinterpret_cast<int4 *>(m.rfl + kBatchStages * kNNMax);
   m.meta = reinterpret_cast<PMeta *>(m.tinfo + kBatchStages);
+  m.field = reinterpret_cast<BatchField *>(m.meta + kBatchStages);
   return m;
 }
 
@@ -137,11 +161,26 @@ __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u
 
 // stage tile u of field `field` into stage st; the tile info's z holds
 // hi_x | lean << 1 | n << 2 and w the field
-template <int MODE, int H>
-__device__ __forceinline__ void bstage_any(const BatchField *fields, int field, const TileCursor &u, ColKey &ck,
-                                           bool &have_col, SlotCol (&col)[kSptMax], const Smem &m, int st)
+// copy field `field` to the block's shared copy.  Only on a change of field
+// (the same for every thread of the block): a barrier so that no thread still
+// reads the previous copy, the copy, a barrier so that every thread sees it.
+__device__ __forceinline__ void load_field(const BatchField *fields, int field, const Smem &m, int &cached)
 {
-  const BatchField &bf = fields[field];
+  if (field == cached) return;
+  static_assert(sizeof(BatchField) % 8 == 0, "field table entries are whole words");
+  const long long *src = reinterpret_cast<const long long *>(fields + field);
+  long long *dst = reinterpret_cast<long long *>(m.field);
+  __syncthreads();
+  for (int i = threadIdx.x; i < (int)(sizeof(BatchField) / 8); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  cached = field;
+}
+
+template <int MODE, int H>
+__device__ __forceinline__ void bstage_any(int field, const TileCursor &u, ColKey &ck, bool &have_col,
+                                           SlotCol (&col)[kSptMax], const Smem &m, int st)
+{
+  const BatchField &bf = *m.field;
   switch (bf.f.n) {
 #define FACES_BSTAGE(NV) \
   case NV: bstage<NV, MODE, H>(bf, u, ck, have_col, col, m, st); break;
@@ -162,27 +201,27 @@ __device__ __forceinline__ void bstage_any(const BatchField *fields, int field, 
 }
 
 template <int MODE, int H>
-__global__ void __launch_bounds__(256, H ? 4 : 3)
-    batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits)
+__global__ void __launch_bounds__(256, bblocks(H))
+    batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits, int run)
 {
   extern __shared__ __align__(16) double sm[];
   const Smem m = smem_layout<H>(sm);
   BWalk nw;  // next tile to stage
-  nw.u = blockIdx.x;
-  nw.done = nw.u >= nunits;
+  nw.done = !bwalk_run(run, nunits, blockIdx.x, nw);
   if (nw.done) return;
   bwalk_unit(fields, units, nw);
   ColKey ck{};
   bool have_col = false;
-  int last_field = -1;
+  int last_field = -1, cached = -1;
   SlotCol col[kSptMax];
   int inflight = 0;
 #pragma unroll
   for (int j = 0; j < kBatchStages - 1; j++) {
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any<MODE, H>(fields, nw.field, nw.cur, ck, have_col, col, m, j);
-      bwalk_next(fields, units, nunits, nw);
+      load_field(fields, nw.field, m, cached);
+      bstage_any<MODE, H>(nw.field, nw.cur, ck, have_col, col, m, j);
+      bwalk_next(fields, units, nunits, run, nw);
       inflight++;
     } else {
       cp_commit();
@@ -202,20 +241,22 @@ __global__ void __launch_bounds__(256, H ? 4 : 3)
     const int sn = (s + kBatchStages - 1) % kBatchStages;
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      bstage_any<MODE, H>(fields, nw.field, nw.cur, ck, have_col, col, m, sn);
-      bwalk_next(fields, units, nunits, nw);
+      load_field(fields, nw.field, m, cached);
+      bstage_any<MODE, H>(nw.field, nw.cur, ck, have_col, col, m, sn);
+      bwalk_next(fields, units, nunits, run, nw);
       inflight++;
     } else {
       cp_commit();
     }
     double *buf = m.data + (long)s * kStage<H>;
+    double *const fu = m.meta[s].u;  // the field of this tile (periodic step)
     // periodic step: x pairs, barrier, y/z pairs (each storing its finals);
     // general step: sums (with their own barriers), barrier, store
     if (nk > 0) {
       switch (n) {
 #define FACES_BSUM(NV)                                                       \
   case NV:                                                                   \
-    if (lean) ptile::pxpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk, threadIdx.x); \
+    if (lean) ptile::pxpass<NV, bk(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);             \
     else sum_tile<NV, bk(NV, H)>(buf, rfl, nk, hx, regular != 0);               \
     break;
         FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
@@ -230,7 +271,7 @@ __global__ void __launch_bounds__(256, H ? 4 : 3)
 #define FACES_BSTORE(NV)                                                                                  \
   case NV:                                                                                                 \
     if (lean)                                                                                              \
-      ptile::pyzpass<NV, bk(NV, H)>(fields[ti.w].f, buf, m.meta + s, nk, threadIdx.x);                     \
+      ptile::pyzpass<NV, bk(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);                                 \
     else                                                                                                   \
       store_tile<NV, bk(NV, H), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;
@@ -256,7 +297,7 @@ RowPlan batch_plan(const FieldDesc &f, int half)
 
 int batch_blocks_per_sm(int half)
 {
-  return std::max(1, std::min(half ? 4 : 3, (int)((228 * 1024) / (batch_smem_bytes(half) + 1024))));
+  return std::max(1, std::min(bblocks(half), (int)((228 * 1024) / (batch_smem_bytes(half) + 1024))));
 }
 
 cudaError_t batch_configure()
@@ -266,6 +307,9 @@ cudaError_t batch_configure()
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, s0);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, s0);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(batch_kernel<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)batch_smem_bytes(2));
   return e;
 }
 
@@ -284,16 +328,19 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
     for (long col = 0; col < ncol; col++) units.push_back({field, (int)col, c0, std::min(c0 + uc, p.nchunks)});
 }
 
-cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
-                         int half, cudaStream_t s)
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int run,
+                         int mode, int half, cudaStream_t s)
 {
+  if (run < 1) run = 1;
   if (nunits <= 0 || grid <= 0) return cudaSuccess;
   if (half && mode != 1) return cudaErrorInvalidValue;  // half-length tiles: periodic step only
   const size_t smem = batch_smem_bytes(half);
-  if (mode == 1 && half) batch_kernel<1, 1><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
-  else if (mode == 1) batch_kernel<1, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
-  else if (mode == 2) batch_kernel<2, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
-  else batch_kernel<0, 0><<<(unsigned)grid, 256, smem, s>>>(d_fields, d_units, nunits);
+  const unsigned g = (unsigned)grid;
+  if (mode == 1 && half == 2) batch_kernel<1, 2><<<g, 256, smem, s>>>(d_fields, d_units, nunits, run);
+  else if (mode == 1 && half) batch_kernel<1, 1><<<g, 256, smem, s>>>(d_fields, d_units, nunits, run);
+  else if (mode == 1) batch_kernel<1, 0><<<g, 256, smem, s>>>(d_fields, d_units, nunits, run);
+  else if (mode == 2) batch_kernel<2, 0><<<g, 256, smem, s>>>(d_fields, d_units, nunits, run);
+  else batch_kernel<0, 0><<<g, 256, smem, s>>>(d_fields, d_units, nunits, run);
   return cudaGetLastError();
 }
 
@@ -331,8 +378,9 @@ struct faces_batch {
   BatchField *d_fields = nullptr;
   BatchUnit *d_units = nullptr;
   int nunits = 0;
+  int run = 8;  // units a block takes in a row
   int mode = 0;      // batch_mode of the fused fields
-  int half = 0;      // half-length tiles (mode 1 only), 4 blocks per SM
+  int half = 0;      // tile length form (mode 1 only): 0 default, 1 half (4 blocks/SM), 2 long (2 blocks/SM)
   int unit_div = 2;  // units are 1/unit_div of a column's chunks
   int per_sm = 3;
   int sms = 0;
@@ -371,6 +419,8 @@ int build_units(faces_batch *b)
     fused.push_back(b->h_fields[i]);
   }
   b->mode = batch_mode(fused.data(), fused.size());
+  if (b->mode != 1 && b->half) return fail(FACES_EINVAL, "faces_batch: half-length tiles need all fields periodic");
+  b->grid = std::min<long>((long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half)), std::max(1, (int)units.size()));
   cudaFree(b->d_units);
   b->d_units = nullptr;
   b->nunits = (int)units.size();
@@ -379,8 +429,9 @@ int build_units(faces_batch *b)
     CUDA_TRY(cudaMemcpy(b->d_units, units.data(), sizeof(BatchUnit) * units.size(), cudaMemcpyHostToDevice),
              "faces_batch: work list upload");
   }
-  if (b->mode != 1 && b->half) return fail(FACES_EINVAL, "faces_batch: half-length tiles need all fields periodic");
-  b->grid = std::min<long>((long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half)), std::max(1, b->nunits));
+  // blocks beyond the runs have nothing to do
+  const long runs = ((long)units.size() + b->run - 1) / b->run;
+  b->grid = std::max(1L, std::min(b->grid, runs));
   drop_graphs(b);
   return FACES_OK;
 }
@@ -399,7 +450,8 @@ int set_half(faces_batch *b, int half)
 
 int launch_batched(faces_batch *b, cudaStream_t s)
 {
-  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->mode, b->half, s), "batch kernel launch");
+  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->run, b->mode, b->half, s),
+           "batch kernel launch");
   return FACES_OK;
 }
 
@@ -529,8 +581,9 @@ int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half)
 {
   if (int rc = check_batch(b, true)) return rc;
   if (half > 0 && b->mode != 1) return fail(FACES_EINVAL, "half-length tiles need every batched field periodic");
+  if (half > 2) return fail(FACES_EINVAL, "half = %d: 0, 1 or 2", half);
   if (half >= 0 && half != b->half)
-    if (int rc = set_half(b, half ? 1 : 0)) return rc;
+    if (int rc = set_half(b, half)) return rc;
   if (unit_div > 0) b->unit_div = unit_div;
   if (blocks_per_sm > 0) b->per_sm = blocks_per_sm;
   return build_units(b);
@@ -544,25 +597,27 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
   // candidates: tile length (full, or half when every field is periodic),
   // units per column, resident blocks per SM (the most that fit, one fewer)
   struct Cand {
-    int half, div, per_sm;
+    int half, div, per_sm, run;
   };
   std::vector<Cand> cands;
   const int divs[] = {1, 2, 4, 8, 64};
-  for (int h = 0; h < (b->mode == 1 ? 2 : 1); h++)
+  const int runs[] = {1, 8};
+  for (int h = 0; h < (b->mode == 1 ? 3 : 1); h++)
     for (int d : divs)
       for (int sm = batch_blocks_per_sm(h); sm >= std::max(1, batch_blocks_per_sm(h) - 1); sm--)
-        cands.push_back({h, d, sm});
+        for (int r : runs) cands.push_back({h, d, sm, r});
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
   CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
   float best = 1e30f;
-  Cand pick{b->half, b->unit_div, b->per_sm};
+  Cand pick{b->half, b->unit_div, b->per_sm, b->run};
   int applied = 0;  // shares the timed launches applied to each batched field
   int rc = FACES_OK;
   for (const Cand &c : cands) {
     if (c.half != b->half && (rc = set_half(b, c.half))) break;
     b->unit_div = c.div;
     b->per_sm = c.per_sm;
+    b->run = c.run;
     if ((rc = build_units(b))) break;
     if (b->nunits == 0) break;
     if ((rc = launch_batched(b, s))) break;  // warm-up
@@ -589,12 +644,13 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
   if (pick.half != b->half && (rc = set_half(b, pick.half))) return rc;
   b->unit_div = pick.div;
   b->per_sm = pick.per_sm;
+  b->run = pick.run;
   if ((rc = build_units(b))) return rc;
   return applied;
 }
 
 int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks,
-                     int *half)
+                     int *half, int *run)
 {
   if (!b) return fail(FACES_EINVAL, "null batch");
   int fu = 0;
@@ -605,6 +661,7 @@ int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *
   if (unit_div) *unit_div = b->unit_div;
   if (blocks) *blocks = (int)b->grid;
   if (half) *half = b->half;
+  if (run) *run = b->run;
   return FACES_OK;
 }
 

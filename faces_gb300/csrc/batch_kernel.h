@@ -45,9 +45,10 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
 // the kernel form for a field table: 0 all general, 1 all periodic (lean), 2 mixed
 int batch_mode(const BatchField *fields, size_t n);
 
-// one share of every field the units cover; grid blocks stride over the
-// units; half = 1 only with mode 1 and plans from batch_plan(f, 1)
-cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int mode,
-                         int half, cudaStream_t s);
+// one share of every field the units cover; blocks take runs of `run`
+// consecutive units (block b: runs b, b + grid, ...); half = 1 or 2 only with
+// mode 1 and plans from batch_plan(f, half)
+cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int run,
+                         int mode, int half, cudaStream_t s);
 
 }  // namespace faces

@@ -29,6 +29,8 @@ namespace faces {
 struct PMeta {
   long off[4];
   long lo[4];
+  double *u;  // the field (so that a tile's sums need no global read)
+  double *pad;
 };
 
 // a field whose tiles the periodic step takes
@@ -121,9 +123,12 @@ __device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
 
 // Stage tile u: the needed pieces of its elements, and the x-lower ends.
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, const TileCursor &u, double *buf,
+__device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPlan &p, const TileCursor &u, double *buf,
                                        PMeta *meta, int4 *tinfo, int t)
 {
+  // one copy of the description (the batched kernel reads it from global
+  // memory; stores through double pointers must not force it to reload)
+  const FieldDesc f = fd;
   constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
   constexpr int KT = PSlots<N, T>::KT, SPT = PSlots<N, T>::SPT;
   constexpr long N3 = (long)N * N * N;
@@ -135,6 +140,7 @@ __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, con
     meta->off[t] = col_off<N>(f, u, t, false, jx0);
     meta->lo[t] = col_off<N>(f, u, t, first, jxl);
   }
+  if (t == 4) meta->u = f.u;
   if (t == 0) *tinfo = make_int4(jx0, nk, 0, 0);
   const long o0 = col_off<N>(f, u, 0, false, jx0), o1 = col_off<N>(f, u, 1, false, jx0);
   const long o2 = col_off<N>(f, u, 2, false, jx0), o3 = col_off<N>(f, u, 3, false, jx0);
@@ -168,7 +174,7 @@ __device__ __forceinline__ void pstage(const FieldDesc &f, const RowPlan &p, con
 // The order is the general step's (x, then y, then z pairs) and every stored
 // cell is one the general step stores, without the unchanged ones.
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PMeta *meta, int nk, int t)
+__device__ __forceinline__ void pxpass(double *__restrict__ u, double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
@@ -184,16 +190,16 @@ __device__ __forceinline__ void pxpass(const FieldDesc &f, double *buf, const PM
     const int sy = r % N, sz = r / N;
     if (sy >= 1 && sy <= N - 2 && sz >= 1 && sz <= N - 2) {
       // interior rows lie in column 0 (the tile's own elements)
-      double *g = f.u + meta->off[0] + k * N3 + sz * NN + sy * N;
+      double *g = u + meta->off[0] + k * N3 + sz * NN + sy * N;
       g[0] = s;
-      if (k == 0) f.u[meta->lo[0] + sz * NN + sy * N + (N - 1)] = s;
+      if (k == 0) u[meta->lo[0] + sz * NN + sy * N + (N - 1)] = s;
       else g[-N3 + (N - 1)] = s;
     }
   }
 }
 
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pyzpass(const FieldDesc &f, const double *buf, const PMeta *meta, int nk, int t)
+__device__ __forceinline__ void pyzpass(double *__restrict__ u, const double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
@@ -220,7 +226,7 @@ __device__ __forceinline__ void pyzpass(const FieldDesc &f, const double *buf, c
     }
     const bool store = lo || c != last_c;
     const long *offs = lo ? meta->lo : meta->off;
-    auto gaddr = [&](int sy, int sz) { return f.u + offs[col_sel<N>(sy, sz)] + gcol + sz * NN + sy * N; };
+    auto gaddr = [&](int sy, int sz) { return u + offs[col_sel<N>(sy, sz)] + gcol + sz * NN + sy * N; };
     if (g < 2 * (N - 2)) {
       int ay, az, by, bz;
       if (g < N - 2) { ay = N - 1; by = 0; az = bz = 1 + g; }              // y pair

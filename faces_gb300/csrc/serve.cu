@@ -68,6 +68,8 @@ int fail(int code, const char *fmt, ...)
 constexpr int kDepth = 2;  // ticks in flight
 // work units of one x-chunk each (units of a job listed chunk group first)
 constexpr int kServeUnitDiv = 64;
+// units a block takes in a row (see launch_batch)
+constexpr int kServeRun = 8;
 
 enum JobState { kQueued = 0, kRunning = 1, kDone = 2, kReleased = 3 };
 
@@ -296,8 +298,11 @@ int rebuild_tables(faces_server *s, Tick &t)
     append_units(units, (int)fields.size(), job.p, kServeUnitDiv);
     fields.push_back({job.f, job.p, ptile_field(job.f) ? 1 : 0});
   }
+  const long runs = ((long)units.size() + kServeRun - 1) / kServeRun;
+  const long grid = std::max(1L, std::min<long>((long)s->sms * s->per_sm, runs));
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;
-  const size_t bytes = fbytes + units.size() * sizeof(BatchUnit);
+  const size_t ubytes = units.size() * sizeof(BatchUnit);
+  const size_t bytes = fbytes + ubytes;
   if (t.staging_cap < bytes) {
     // the tick is not in flight, so its last copy from the buffer is done
     if (t.staging) cudaFreeHost(t.staging);
@@ -308,7 +313,7 @@ int rebuild_tables(faces_server *s, Tick &t)
     t.staging_cap = bytes * 2;
   }
   std::memcpy(t.staging, fields.data(), fields.size() * sizeof(BatchField));
-  std::memcpy(t.staging + fbytes, units.data(), units.size() * sizeof(BatchUnit));
+  std::memcpy(t.staging + fbytes, units.data(), ubytes);
   if (s->d_tables) CUDA_TRY(cudaFreeAsync(s->d_tables, s->stream), "server: free work list");
   s->d_tables = nullptr;
   CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void **>(&s->d_tables), bytes, s->pool, s->stream),
@@ -318,7 +323,7 @@ int rebuild_tables(faces_server *s, Tick &t)
   s->tables_fbytes = fbytes;
   s->kmode = batch_mode(fields.data(), fields.size());
   s->nunits = (int)units.size();
-  s->grid = std::min<long>((long)s->sms * s->per_sm, std::max(1, s->nunits));
+  s->grid = grid;
   s->set_changed = false;
   return FACES_OK;
 }
@@ -339,7 +344,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          s->kmode, 0, s->stream),
+                          kServeRun, s->kmode, 0, s->stream),
              "server: batched launch");
     s->launches++;
   }

@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
       cp_commit();
     }
     double *buf = sm + s * stage;
-    ptile::pxpass<N, K>(f, buf, meta + s, nk, threadIdx.x);
+    ptile::pxpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
     __syncthreads();
-    ptile::pyzpass<N, K>(f, buf, meta + s, nk, threadIdx.x);
+    ptile::pyzpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
     s = (s + 1) % NS;
   }
 }
@@ -194,9 +194,9 @@ __global__ void __launch_bounds__(WPB * 32) wtile_kernel(FieldDesc f, RowPlan p)
       cp_commit();
     }
     double *buf = wsm + s * stage;
-    ptile::pxpass<N, K, 32>(f, buf, meta + s, nk, lane);
+    ptile::pxpass<N, K, 32>(f.u, buf, meta + s, nk, lane);
     __syncwarp();
-    ptile::pyzpass<N, K, 32>(f, buf, meta + s, nk, lane);
+    ptile::pyzpass<N, K, 32>(f.u, buf, meta + s, nk, lane);
     s = (s + 1) % NS;
   }
 }

@@ -202,21 +202,23 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream);
 
 /* Work list settings: unit_div (units are 1/unit_div of a column's
  * x-chunks; <= 0 keeps it), resident blocks per SM (<= 0 keeps it), half
- * (1: half-length tiles, whose smaller stages keep 4 blocks per SM; only
- * when every batched field is periodic and in direct mode; < 0 keeps it). */
+ * (tile length: 0 default; 1 half-length tiles, whose smaller stages keep 4
+ * blocks per SM; 2 tiles of up to ~28 KB, 2 blocks per SM; 1 and 2 only when
+ * every batched field is periodic and in direct mode; < 0 keeps it). */
 int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half);
 
-/* Times the batched launch over unit_div in {1,2,4,8,64}, full or
- * half-length tiles (when allowed) and the resident blocks per SM that fit, `trials` launches each (after one warm-up), and
+/* Times the batched launch over unit_div in {1,2,4,8,64}, the tile lengths
+ * (when allowed), runs of 1 or 8 units per block and the resident blocks per SM that fit, `trials` launches each (after one warm-up), and
  * keeps the fastest.  Every launch is a share of the fields in the batched
  * launch (the others are untouched): returns how many shares it applied to
  * each of them (>= 0), or a negative error code.  Synchronous. */
 int faces_batch_autotune(faces_batch *b, int trials, void *stream);
 
 /* fields, fields in the batched launch, work units, unit_div, blocks of the
- * batched launch, half-length tiles (each may be NULL). */
+ * batched launch, tile length form, units a block takes in a row (each may
+ * be NULL). */
 int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks,
-                     int *half);
+                     int *half, int *run);
 
 int faces_batch_destroy(faces_batch *b);
 
