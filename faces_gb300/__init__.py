@@ -97,9 +97,10 @@ def lib() -> ctypes.CDLL:
     L.faces_server_stats.argtypes = [vp, sp]
     L.faces_server_run_trace.argtypes = [vp, c_int, jp, dblp, llp, dblp, dblp]
     L.faces_server_destroy.argtypes = [vp]
+    L.faces_server_tune.argtypes = [vp, c_int, c_int, c_int]
     for name in ("faces_server_create", "faces_server_submit", "faces_server_poll", "faces_server_drain",
                  "faces_server_job_status", "faces_server_field", "faces_server_fetch", "faces_server_release",
-                 "faces_server_stats", "faces_server_run_trace", "faces_server_destroy"):
+                 "faces_server_stats", "faces_server_run_trace", "faces_server_destroy", "faces_server_tune"):
         getattr(L, name).restype = c_int
     for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
                  "faces_share", "faces_share_n", "faces_init_ref", "faces_init_int", "faces_check",
@@ -443,6 +444,10 @@ class Server:
     def release(self, jid: int) -> None:
         _check(lib().faces_server_release(self._h, jid))
         self._inputs.pop(jid, None)
+
+    def tune(self, unit_div: int = 0, run: int = 0, half: int = -1) -> None:
+        """Work list settings of the batched launch (faces_server_tune)."""
+        _check(lib().faces_server_tune(self._h, unit_div, run, half))
 
     def stats(self) -> dict:
         st = ServeStats()

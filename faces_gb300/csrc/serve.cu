@@ -66,10 +66,11 @@ int fail(int code, const char *fmt, ...)
   } while (0)
 
 constexpr int kDepth = 2;  // ticks in flight
-// work units of one x-chunk each (units of a job listed chunk group first)
-constexpr int kServeUnitDiv = 64;
-// units a block takes in a row (see launch_batch)
-constexpr int kServeRun = 8;
+// work units of whole columns, one per block in a row (see launch_batch):
+// the fastest of the settings timed on the served workload (1.56x the plain
+// form saturated; one-chunk units and runs of 8 gave 1.43-1.44x)
+constexpr int kServeUnitDiv = 1;
+constexpr int kServeRun = 1;
 
 enum JobState { kQueued = 0, kRunning = 1, kDone = 2, kReleased = 3 };
 
@@ -121,6 +122,7 @@ struct faces_server {
   size_t tables_fbytes = 0;
   int nunits = 0;
   int kmode = 0;  // batch_mode of the running set
+  int unit_div = kServeUnitDiv, run = kServeRun, half = 0;  // work list settings (faces_server_tune)
   long grid = 0;
   Tick ticks[kDepth];
   int tick_head = 0, in_flight = 0;  // ring of in-flight ticks
@@ -210,7 +212,7 @@ int admit(faces_server *s, Job &job)
   f.msg = nullptr;
   f.msg_off = nullptr;
   f.nbr = nbr;
-  job.p = batch_plan(f, 0);
+  job.p = batch_plan(f, s->half);
   plain_plan(s, job);
   cudaError_t e;
   if (j.init == 0) e = launch_init_ref(f, s->stream);
@@ -295,10 +297,10 @@ int rebuild_tables(faces_server *s, Tick &t)
   fields.reserve(order.size());
   for (long long id : order) {
     const Job &job = s->jobs[id];
-    append_units(units, (int)fields.size(), job.p, kServeUnitDiv);
+    append_units(units, (int)fields.size(), job.p, s->unit_div);
     fields.push_back({job.f, job.p, ptile_field(job.f) ? 1 : 0});
   }
-  const long runs = ((long)units.size() + kServeRun - 1) / kServeRun;
+  const long runs = ((long)units.size() + s->run - 1) / s->run;
   const long grid = std::max(1L, std::min<long>((long)s->sms * s->per_sm, runs));
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;
   const size_t ubytes = units.size() * sizeof(BatchUnit);
@@ -344,7 +346,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          kServeRun, s->kmode, 0, s->stream),
+                          s->run, s->kmode, s->kmode == 1 ? s->half : 0, s->stream),
              "server: batched launch");
     s->launches++;
   }
@@ -529,6 +531,21 @@ int faces_server_release(faces_server *s, long long id)
     return fail(FACES_EINVAL, "job %lld is not done (state %d)", id, j->state);
   if (int rc = release_job(s, *j)) return rc;
   s->jobs.erase(id);
+  return FACES_OK;
+}
+
+int faces_server_tune(faces_server *s, int unit_div, int run, int half)
+{
+  if (!s) return fail(FACES_EINVAL, "null server");
+  if (half > 2) return fail(FACES_EINVAL, "half = %d: 0, 1 or 2", half);
+  if (half >= 0 && half != s->half) {
+    if (!s->jobs.empty()) return fail(FACES_EINVAL, "the tile form is set before the first job");
+    s->half = half;
+    s->per_sm = batch_blocks_per_sm(half);
+  }
+  if (unit_div > 0) s->unit_div = unit_div;
+  if (run > 0) s->run = run;
+  s->set_changed = true;
   return FACES_OK;
 }
 
