@@ -78,7 +78,6 @@ struct Job {
   long long id = 0;
   faces_job spec{};
   FieldDesc f{};
-  RowPlan p{};     // batched kernel plan
   RowPlan tp{};    // single-field tile plan (plain form)
   long tgrid = 0;  // single-field tile kernel blocks (plain form)
   size_t bytes = 0;
@@ -106,7 +105,7 @@ struct faces_server {
   size_t budget = 0, resident = 0, peak_resident = 0;
   int max_jobs = 0;
   unsigned flags = 0;
-  int sms = 0, per_sm = 1;
+  int sms = 0;
   cudaStream_t stream = nullptr, fetch_stream = nullptr;
   cudaMemPool_t pool = nullptr;
   cudaEvent_t base = nullptr;
@@ -121,7 +120,7 @@ struct faces_server {
   char *d_tables = nullptr;
   size_t tables_fbytes = 0;
   int nunits = 0;
-  int kmode = 0;  // batch_mode of the running set
+  int kmode = 0, khalf = 0;  // kernel form of the running set's work list
   int unit_div = kServeUnitDiv, run = kServeRun, half = 0;  // work list settings (faces_server_tune)
   long grid = 0;
   Tick ticks[kDepth];
@@ -212,7 +211,6 @@ int admit(faces_server *s, Job &job)
   f.msg = nullptr;
   f.msg_off = nullptr;
   f.nbr = nbr;
-  job.p = batch_plan(f, s->half);
   plain_plan(s, job);
   cudaError_t e;
   if (j.init == 0) e = launch_init_ref(f, s->stream);
@@ -292,16 +290,23 @@ int rebuild_tables(faces_server *s, Tick &t)
   std::vector<long long> order = s->running;
   std::stable_sort(order.begin(), order.end(),
                    [&](long long a, long long b) { return s->jobs[a].f.n < s->jobs[b].f.n; });
+  // the kernel form: the tile form applies only when every job takes the
+  // periodic step; plans are made for the form that runs
+  int lean = 0;
+  for (long long id : order) lean += ptile_field(s->jobs[id].f) ? 1 : 0;
+  const int kmode = lean == 0 ? 0 : lean == (int)order.size() ? 1 : 2;
+  const int half = kmode == 1 ? s->half : 0;
   std::vector<BatchField> fields;
   std::vector<BatchUnit> units;
   fields.reserve(order.size());
   for (long long id : order) {
     const Job &job = s->jobs[id];
-    append_units(units, (int)fields.size(), job.p, s->unit_div);
-    fields.push_back({job.f, job.p, ptile_field(job.f) ? 1 : 0});
+    const RowPlan p = batch_plan(job.f, half);
+    append_units(units, (int)fields.size(), p, s->unit_div);
+    fields.push_back({job.f, p, ptile_field(job.f) ? 1 : 0});
   }
   const long runs = ((long)units.size() + s->run - 1) / s->run;
-  const long grid = std::max(1L, std::min<long>((long)s->sms * s->per_sm, runs));
+  const long grid = std::max(1L, std::min<long>((long)s->sms * batch_blocks_per_sm(half), runs));
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;
   const size_t ubytes = units.size() * sizeof(BatchUnit);
   const size_t bytes = fbytes + ubytes;
@@ -323,7 +328,8 @@ int rebuild_tables(faces_server *s, Tick &t)
   CUDA_TRY(cudaMemcpyAsync(s->d_tables, t.staging, bytes, cudaMemcpyHostToDevice, s->stream),
            "server: work list upload");
   s->tables_fbytes = fbytes;
-  s->kmode = batch_mode(fields.data(), fields.size());
+  s->kmode = kmode;
+  s->khalf = half;
   s->nunits = (int)units.size();
   s->grid = grid;
   s->set_changed = false;
@@ -346,7 +352,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          s->run, s->kmode, s->kmode == 1 ? s->half : 0, s->stream),
+                          s->run, s->kmode, s->khalf, s->stream),
              "server: batched launch");
     s->launches++;
   }
@@ -460,7 +466,6 @@ int faces_server_create(faces_server **out, size_t budget_bytes, int max_jobs, u
     return fail(FACES_ECUDA, "faces_server_create: %s", cudaGetErrorString(e));
   }
   s->base_host = host_seconds();
-  s->per_sm = batch_blocks_per_sm(0);
   *out = s;
   return FACES_OK;
 }
@@ -538,11 +543,7 @@ int faces_server_tune(faces_server *s, int unit_div, int run, int half)
 {
   if (!s) return fail(FACES_EINVAL, "null server");
   if (half > 2) return fail(FACES_EINVAL, "half = %d: 0, 1 or 2", half);
-  if (half >= 0 && half != s->half) {
-    if (!s->jobs.empty()) return fail(FACES_EINVAL, "the tile form is set before the first job");
-    s->half = half;
-    s->per_sm = batch_blocks_per_sm(half);
-  }
+  if (half >= 0) s->half = half;
   if (unit_div > 0) s->unit_div = unit_div;
   if (run > 0) s->run = run;
   s->set_changed = true;

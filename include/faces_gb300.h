@@ -296,7 +296,7 @@ int faces_server_stats(const faces_server *s, faces_serve_stats *st);
 /* Work list settings of the batched launch (as faces_batch_tune): unit_div
  * (units are 1/unit_div of a column's x-chunks; default 1, whole columns),
  * run (units a block takes in a row; default 1), half (tile form 0, 1 or 2;
- * only before the first job; used when every running job is periodic).
+ * used for ticks in which every running job is periodic, else 0).
  * Values <= 0 (half < 0) keep the setting. */
 int faces_server_tune(faces_server *s, int unit_div, int run, int half);
 

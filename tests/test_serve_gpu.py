@@ -48,11 +48,16 @@ def alone(F, j):
     return out
 
 
-@pytest.mark.parametrize("plain", [False, True], ids=["batched", "plain"])
-def test_results_equal_alone(faces_lib, plain):
+@pytest.mark.parametrize("form", ["batched", "plain", "chunk_units_runs8", "long_tiles", "half_tiles"])
+def test_results_equal_alone(faces_lib, form):
+    """A mix of periodic and open jobs: ticks switch between the periodic-only
+    kernel form (where the tile form applies) and the mixed one."""
     F = faces_lib
     jobs = random_jobs(F, 24, seed=1)
-    with F.Server(4 * GB, plain=plain) as srv:
+    tune = {"chunk_units_runs8": (64, 8, 0), "long_tiles": (1, 8, 2), "half_tiles": (2, 1, 1)}.get(form)
+    with F.Server(4 * GB, plain=form == "plain") as srv:
+        if tune:
+            srv.tune(*tune)
         ids = [srv.submit(j) for j in jobs]
         srv.drain()
         st = srv.stats()
