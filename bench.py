@@ -484,6 +484,7 @@ def profile_c4(F, shares: int) -> dict:
     for f, u in fields:
         b.add(f, u)
     b.commit()
+    b.tune(1, 0, 0, 1)  # whole-column units, full tiles, one unit per run: faces_batch_autotune's pick
     for _ in range(shares):
         b.share()
     torch.cuda.synchronize()

@@ -80,7 +80,7 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_share.argtypes = [vp, c_int, vp]
     L.faces_batch_share_n.argtypes = [vp, c_int, c_int, vp]
     L.faces_batch_share_each.argtypes = [vp, c_int, vp]
-    L.faces_batch_tune.argtypes = [vp, c_int, c_int, c_int]
+    L.faces_batch_tune.argtypes = [vp, c_int, c_int, c_int, c_int]
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
     L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
@@ -354,8 +354,8 @@ class Batch:
     def share_each(self, compute: bool = True, stream=None) -> None:
         _check(lib().faces_batch_share_each(self._h, int(compute), _stream(stream)))
 
-    def tune(self, unit_div: int = 0, blocks_per_sm: int = 0, half: int = -1) -> None:
-        _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm, half))
+    def tune(self, unit_div: int = 0, blocks_per_sm: int = 0, half: int = -1, run: int = 0) -> None:
+        _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm, half, run))
 
     def autotune(self, trials: int = 3, stream=None) -> int:
         """Keeps the fastest work split; returns the shares it applied to

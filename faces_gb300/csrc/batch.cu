@@ -577,7 +577,7 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream)
   return share_others(b, compute, true, stream);
 }
 
-int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half)
+int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half, int run)
 {
   if (int rc = check_batch(b, true)) return rc;
   if (half > 0 && b->mode != 1) return fail(FACES_EINVAL, "half-length tiles need every batched field periodic");
@@ -586,6 +586,7 @@ int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half)
     if (int rc = set_half(b, half)) return rc;
   if (unit_div > 0) b->unit_div = unit_div;
   if (blocks_per_sm > 0) b->per_sm = blocks_per_sm;
+  if (run > 0) b->run = run;
   return build_units(b);
 }
 

@@ -204,8 +204,9 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream);
  * x-chunks; <= 0 keeps it), resident blocks per SM (<= 0 keeps it), half
  * (tile length: 0 default; 1 half-length tiles, whose smaller stages keep 4
  * blocks per SM; 2 tiles of up to ~28 KB, 2 blocks per SM; 1 and 2 only when
- * every batched field is periodic and in direct mode; < 0 keeps it). */
-int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half);
+ * every batched field is periodic and in direct mode; < 0 keeps it), run
+ * (units a block takes in a row before striding by the grid; <= 0 keeps it). */
+int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half, int run);
 
 /* Times the batched launch over unit_div in {1,2,4,8,64}, the tile lengths
  * (when allowed), runs of 1 or 8 units per block and the resident blocks per SM that fit, `trials` launches each (after one warm-up), and

@@ -86,7 +86,7 @@ def test_batch_equals_alone(faces_lib, how, compute):
         assert np.array_equal(a, b), f"field {i} {MIX[i]}"
 
 
-@pytest.mark.parametrize("tune", [(1, 1), (2, 2), (4, 3), (8, 0), (64, 1)], ids=str)
+@pytest.mark.parametrize("tune", [(1, 1), (2, 2, -1, 3), (4, 3), (8, 0, -1, 1), (64, 1, -1, 8)], ids=str)
 def test_batch_work_split(faces_lib, tune):
     F = faces_lib
     ref = alone(F, MIX, 2)
