@@ -17,8 +17,9 @@
 //                    and written in place) or message mode (v-26: remote
 //                    copies read from the 26 received messages, each rank
 //                    writes only its own copies).
-//   gather_kernel    the step for any n and compute=false: one thread per
-//                    owned shared point gathers its copies.
+//   gather_kernel    the step for any n: one thread per owned shared point
+//                    gathers its copies; boundary_gather_kernel the same for
+//                    the subdomain-boundary points only (compute = false).
 //   pack_kernel      message mode: the 26 raw boundary messages of every rank
 //                    (gpu/v-26-messages/Faces.cc:243-293).
 //   init_*_kernel    gpu/main.cc:10-19 formula, or seeded integer values.
@@ -146,9 +147,78 @@ __device__ __forceinline__ void local_axis(int g, int n, Copies &c)
   c.cnt = 2; c.e[0] = E - 1; c.i[0] = nm1; c.e[1] = E; c.i[1] = 0;
 }
 
-__global__ void gather_kernel(FieldDesc f, int compute)
+// One shared point: point g (global in rank r's subdomain) and its copies,
+// summed as a tree x, y, z and written to every local copy.  Points that are
+// not shared, or that another rank owns (direct mode), return at once.
+__device__ __forceinline__ void gather_point(const FieldDesc &f, int r, const int g[3], int compute)
 {
   const int n = f.n, nm1 = n - 1;
+  // a point is shared only if it lies on an element boundary somewhere
+  if (g[0] % nm1 && g[1] % nm1 && g[2] % nm1) return;
+  bool onb = false, skip = false;
+  Copies c[3];
+  for (int a = 0; a < 3; a++) {
+    const int Ga = f.m[a] * nm1;
+    onb |= (g[a] == 0 || g[a] == Ga);
+    int up[3] = {0, 0, 0};
+    up[a] = 1;
+    // direct mode: the upper rank owns the points of the shared plane
+    if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(up[0], up[1], up[2])) >= 0) skip = true;
+    local_axis(g[a], n, c[a]);
+    // drop copies whose neighbour rank does not exist
+    int k = 0;
+    for (int b = 0; b < c[a].cnt; b++) {
+      const int e = c[a].e[b];
+      int dv[3] = {0, 0, 0};
+      dv[a] = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
+      if (dv[a] && nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) < 0) continue;
+      c[a].e[k] = e; c[a].i[k] = c[a].i[b]; k++;
+    }
+    c[a].cnt = k;
+  }
+  if (skip) return;
+  if (c[0].cnt * c[1].cnt * c[2].cnt < 2) return;
+  if (!compute && !onb) return;
+  double v[2][2][2];
+  double *w[2][2][2];
+  for (int bz = 0; bz < c[2].cnt; bz++)
+    for (int by = 0; by < c[1].cnt; by++)
+      for (int bx = 0; bx < c[0].cnt; bx++) {
+        int e[3] = {c[0].e[bx], c[1].e[by], c[2].e[bz]};
+        const int i[3] = {c[0].i[bx], c[1].i[by], c[2].i[bz]};
+        int d[3], j[3];
+        for (int a = 0; a < 3; a++) {
+          d[a] = e[a] < 0 ? -1 : (e[a] >= f.m[a] ? 1 : 0);
+          j[a] = e[a] < 0 ? f.m[a] - 1 : (e[a] >= f.m[a] ? 0 : e[a]);
+        }
+        const int dir = dir_index(d[0], d[1], d[2]);
+        if (dir == 13 || f.mode == kDirect) {
+          const int q = (dir == 13) ? r : nbr_of(f, r, dir);
+          double *ptr = f.u + (long)q * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
+          w[bz][by][bx] = ptr;
+          v[bz][by][bx] = *ptr;
+        } else {
+          const double *rb = recv_of(f, r, dir);
+          w[bz][by][bx] = nullptr;
+          v[bz][by][bx] = rb[region_pos(f, d, i, j)];
+        }
+      }
+  double sy[2];
+  for (int bz = 0; bz < c[2].cnt; bz++) {
+    double sx[2];
+    for (int by = 0; by < c[1].cnt; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
+    sy[bz] = (c[1].cnt == 2) ? sx[0] + sx[1] : sx[0];
+  }
+  const double s = (c[2].cnt == 2) ? sy[0] + sy[1] : sy[0];
+  for (int bz = 0; bz < c[2].cnt; bz++)
+    for (int by = 0; by < c[1].cnt; by++)
+      for (int bx = 0; bx < c[0].cnt; bx++)
+        if (w[bz][by][bx]) *w[bz][by][bx] = s;
+}
+
+__global__ void gather_kernel(FieldDesc f, int compute)
+{
+  const int nm1 = f.n - 1;
   const long G0 = (long)f.m[0] * nm1 + 1, G1 = (long)f.m[1] * nm1 + 1, G2 = (long)f.m[2] * nm1 + 1;
   const long per_rank = G0 * G1 * G2;
   const long total = per_rank * f.nranks;
@@ -156,67 +226,49 @@ __global__ void gather_kernel(FieldDesc f, int compute)
     const int r = (int)(p / per_rank);
     long t = p % per_rank;
     const int g[3] = {(int)(t % G0), (int)((t / G0) % G1), (int)(t / (G0 * G1))};
-    // a point is shared only if it lies on an element boundary somewhere
-    if (g[0] % nm1 && g[1] % nm1 && g[2] % nm1) continue;
-    bool onb = false, skip = false;
-    Copies c[3];
-    for (int a = 0; a < 3; a++) {
-      const int Ga = f.m[a] * nm1;
-      onb |= (g[a] == 0 || g[a] == Ga);
-      int up[3] = {0, 0, 0};
-      up[a] = 1;
-      // direct mode: the upper rank owns the points of the shared plane
-      if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(up[0], up[1], up[2])) >= 0) skip = true;
-      local_axis(g[a], n, c[a]);
-      // drop copies whose neighbour rank does not exist
-      int k = 0;
-      for (int b = 0; b < c[a].cnt; b++) {
-        const int e = c[a].e[b];
-        int dv[3] = {0, 0, 0};
-        dv[a] = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
-        if (dv[a] && nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) < 0) continue;
-        c[a].e[k] = e; c[a].i[k] = c[a].i[b]; k++;
-      }
-      c[a].cnt = k;
+    gather_point(f, r, g, compute);
+  }
+}
+
+// compute = 0: only points on the subdomain boundary are summed, so enumerate
+// just those: the two z faces, the two y faces without their z edges, the
+// two x faces without their y and z edges (G0*G1*G2 - (G0-2)(G1-2)(G2-2)
+// points per rank)
+__host__ __device__ __forceinline__ long boundary_points(long G0, long G1, long G2)
+{
+  return 2 * G0 * G1 + 2 * G0 * (G2 - 2) + 2 * (G1 - 2) * (G2 - 2);
+}
+
+__global__ void boundary_gather_kernel(FieldDesc f)
+{
+  const int nm1 = f.n - 1;
+  const long G0 = (long)f.m[0] * nm1 + 1, G1 = (long)f.m[1] * nm1 + 1, G2 = (long)f.m[2] * nm1 + 1;
+  const long per_rank = boundary_points(G0, G1, G2);
+  const long total = per_rank * f.nranks;
+  const long fz = 2 * G0 * G1, fy = 2 * G0 * (G2 - 2);
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(p / per_rank);
+    long t = p - (long)r * per_rank;
+    int g[3];
+    if (t < fz) {
+      const long side = t / (G0 * G1), q = t - side * G0 * G1;
+      g[0] = (int)(q % G0);
+      g[1] = (int)(q / G0);
+      g[2] = side ? (int)(G2 - 1) : 0;
+    } else if (t < fz + fy) {
+      t -= fz;
+      const long side = t / (G0 * (G2 - 2)), q = t - side * G0 * (G2 - 2);
+      g[0] = (int)(q % G0);
+      g[2] = 1 + (int)(q / G0);
+      g[1] = side ? (int)(G1 - 1) : 0;
+    } else {
+      t -= fz + fy;
+      const long side = t / ((G1 - 2) * (G2 - 2)), q = t - side * (G1 - 2) * (G2 - 2);
+      g[1] = 1 + (int)(q % (G1 - 2));
+      g[2] = 1 + (int)(q / (G1 - 2));
+      g[0] = side ? (int)(G0 - 1) : 0;
     }
-    if (skip) continue;
-    if (c[0].cnt * c[1].cnt * c[2].cnt < 2) continue;
-    if (!compute && !onb) continue;
-    double v[2][2][2];
-    double *w[2][2][2];
-    for (int bz = 0; bz < c[2].cnt; bz++)
-      for (int by = 0; by < c[1].cnt; by++)
-        for (int bx = 0; bx < c[0].cnt; bx++) {
-          int e[3] = {c[0].e[bx], c[1].e[by], c[2].e[bz]};
-          const int i[3] = {c[0].i[bx], c[1].i[by], c[2].i[bz]};
-          int d[3], j[3];
-          for (int a = 0; a < 3; a++) {
-            d[a] = e[a] < 0 ? -1 : (e[a] >= f.m[a] ? 1 : 0);
-            j[a] = e[a] < 0 ? f.m[a] - 1 : (e[a] >= f.m[a] ? 0 : e[a]);
-          }
-          const int dir = dir_index(d[0], d[1], d[2]);
-          if (dir == 13 || f.mode == kDirect) {
-            const int q = (dir == 13) ? r : nbr_of(f, r, dir);
-            double *ptr = f.u + (long)q * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
-            w[bz][by][bx] = ptr;
-            v[bz][by][bx] = *ptr;
-          } else {
-            const double *rb = recv_of(f, r, dir);
-            w[bz][by][bx] = nullptr;
-            v[bz][by][bx] = rb[region_pos(f, d, i, j)];
-          }
-        }
-    double sy[2];
-    for (int bz = 0; bz < c[2].cnt; bz++) {
-      double sx[2];
-      for (int by = 0; by < c[1].cnt; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
-      sy[bz] = (c[1].cnt == 2) ? sx[0] + sx[1] : sx[0];
-    }
-    const double s = (c[2].cnt == 2) ? sy[0] + sy[1] : sy[0];
-    for (int bz = 0; bz < c[2].cnt; bz++)
-      for (int by = 0; by < c[1].cnt; by++)
-        for (int bx = 0; bx < c[0].cnt; bx++)
-          if (w[bz][by][bx]) *w[bz][by][bx] = s;
+    gather_point(f, r, g, 0);
   }
 }
 
@@ -670,7 +722,15 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
 
 cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s)
 {
-  gather_kernel<<<152 * 16, 256, 0, s>>>(f, compute);
+  if (compute) {
+    gather_kernel<<<152 * 16, 256, 0, s>>>(f, compute);
+  } else {
+    const int nm1 = f.n - 1;
+    const long G0 = (long)f.m[0] * nm1 + 1, G1 = (long)f.m[1] * nm1 + 1, G2 = (long)f.m[2] * nm1 + 1;
+    const long total = boundary_points(G0, G1, G2) * f.nranks;
+    const long blocks = (total + 255) / 256;
+    boundary_gather_kernel<<<(unsigned)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, s>>>(f);
+  }
   return cudaGetLastError();
 }
 
