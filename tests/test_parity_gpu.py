@@ -207,3 +207,27 @@ def test_warp_tiles_bit_exact(oracle, faces_lib, shape):
         f.close()
         ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
         assert np.array_equal(out, O.groups_share(s, ref0, True, 3)), init
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1, 15, 14, 13, 12), (2, 2, 1, 9, 7, 5, 11), (1, 2, 2, 11, 6, 7, 10),
+                                   (3, 1, 1, 6, 9, 8, 9), (1, 1, 1, 24, 5, 6, 3)],
+                         ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+@pytest.mark.parametrize("mode", ["tiles", "general", "rows", "messages", "v6"])
+def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
+    """The reference's 15x14x13 n=12 shape and other shapes with every
+    dimension several elements long, every strategy: the device closed form
+    after 3 shares, and equality with the default kernel bit for bit."""
+    F = faces_lib
+    outs = []
+    for m in ("tiles", mode):
+        f = F.Faces(*shape, periodic=periodic, general=m == "general", rows=m == "rows",
+                    messages=m == "messages", v6=m == "v6")
+        u = f.field()
+        f.init_int(u, 9)
+        f.share_n(u, 3)
+        chk = f.check(u, init="int", seed=9, nshares=3)
+        assert chk.passed and chk.maxrel == 0.0, (m, chk)
+        outs.append(u)
+        f.close()
+    assert torch.equal(outs[0], outs[1])
