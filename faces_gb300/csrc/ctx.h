@@ -26,6 +26,8 @@ struct faces_ctx {
   faces::RowPlan plan;   // row kernel
   faces::RowPlan tplan;  // tile kernel
   long tgrid = 0;    // tile kernel CTAs
+  int variant = 0;   // set by faces_autotune: 0 the tile step (periodic or mixed),
+                     // 1 the general tile step, 2 the row kernel
 
   faces::FieldDesc desc(double *u) const
   {

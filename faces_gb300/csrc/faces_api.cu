@@ -236,13 +236,15 @@ int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
   c->chunk = chunk > 0 ? chunk : 0;
   c->tpb = width > 0 ? width : 0;
   c->order = order;
+  c->variant = 0;
   replan(*c);
   return FACES_OK;
 }
 
-int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks)
+int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks, int *kernel)
 {
   if (int rc = check_ctx(c)) return rc;
+  if (kernel) *kernel = c->variant;
   if (chunk) *chunk = c->tplan.chunk;
   if (unit_chunks) *unit_chunks = c->tplan.unit_chunks;
   if (blocks) *blocks = (int)c->tgrid;
@@ -266,12 +268,11 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   }
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   const bool fused = compute && !(c->flags & FACES_GATHER);
-  if (fused && !(c->flags & FACES_ROWS) && tile_kernel_supported(c->n))
-  {
-    if (c->tplan.order == 3) CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
-    else CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, (c->flags & FACES_GENERAL) != 0), "tile kernel launch");
-  }
-  else if (fused && row_kernel_supported(c->n))
+  if (fused && !(c->flags & FACES_ROWS) && c->variant != 2 && tile_kernel_supported(c->n)) {
+    const bool general = (c->flags & FACES_GENERAL) || c->variant == 1;
+    if (c->tplan.order == 3 && !general) CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
+    else CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general), "tile kernel launch");
+  } else if (fused && row_kernel_supported(c->n))
     CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
   else
     CUDA_TRY(launch_gather(f, compute, s), "gather kernel launch");
@@ -312,36 +313,54 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   CUDA_TRY(cudaEventCreate(&e0), "autotune: event");
   CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
   float best = 1e30f;
-  int bk = c->chunk, bo = c->order, bw = c->tpb, applied = 0, rc = FACES_OK;
+  int bk = c->chunk, bo = c->order, bw = c->tpb, bv = c->variant, applied = 0, rc = FACES_OK;
+  // time the current settings (kernel variant v) once; keep the fastest
+  auto trial = [&](int v) {
+    c->variant = v;
+    replan(*c);
+    if ((rc = share_once(c, u, compute, s))) return;  // warm-up
+    cudaEventRecord(e0, s);
+    for (int t = 0; t < trials && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
+    cudaEventRecord(e1, s);
+    applied += 1 + trials;
+    if (rc) return;
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      rc = fail(FACES_ECUDA, "autotune: %s", cudaGetErrorString(e));
+      return;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) { best = ms; bk = c->chunk; bo = c->order; bw = c->tpb; bv = v; }
+  };
+  const bool periodic_step = (c->flags & FACES_PERIODIC) && !(c->flags & (FACES_MESSAGES | FACES_GENERAL));
   for (int ki = 0; ki < 3 && rc == FACES_OK; ki++) {
     if (ks[ki] < 1 || (ki > 0 && ks[ki] == k0)) continue;
     for (int o : orders)
       for (int w : widths) {
         if (rc != FACES_OK) break;
-        if (o == 3 && ki > 0) continue;  // warp tiles have one tile length
+        if (o == 3 && (ki > 0 || !periodic_step)) continue;  // warp tiles: periodic step, one tile length
         c->chunk = ks[ki];
         c->order = o;
         c->tpb = w;
         replan(*c);
         if (ki == 2 && c->tplan.chunk == k0) continue;  // doubling not possible
-        if ((rc = share_once(c, u, compute, s))) break;  // warm-up
-        cudaEventRecord(e0, s);
-        for (int t = 0; t < trials && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
-        cudaEventRecord(e1, s);
-        applied += 1 + trials;
-        if (rc) break;
-        cudaError_t e = cudaEventSynchronize(e1);
-        if (e != cudaSuccess) { rc = fail(FACES_ECUDA, "autotune: %s", cudaGetErrorString(e)); break; }
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) { best = ms; bk = c->chunk; bo = c->order; bw = c->tpb; }
+        trial(0);
       }
   }
+  // the other kernels at their default settings: the general tile step
+  // (where the mixed step runs) and the row kernel
+  c->chunk = 0;
+  c->order = -1;
+  c->tpb = 0;
+  if (rc == FACES_OK && !periodic_step && !(c->flags & FACES_GENERAL)) trial(1);
+  if (rc == FACES_OK && row_kernel_supported(c->n)) trial(2);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   c->chunk = bk;
   c->order = bo;
   c->tpb = bw;
+  c->variant = bv;
   replan(*c);
   return rc ? rc : applied;
 }

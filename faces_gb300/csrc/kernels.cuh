@@ -32,7 +32,8 @@ size_t wtile_smem_bytes(int n);
 int wtile_blocks_per_sm(int n);
 cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);
 
-// periodic direct-mode fields take the periodic tile step unless `general`
+// periodic direct-mode fields take the periodic tile step, other fields the
+// mixed step (periodic step on interior tiles), unless `general`
 cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false);
 
 // Closed-form check of a field after `nshares` shares of a known initial

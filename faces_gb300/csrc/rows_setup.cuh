@@ -122,6 +122,15 @@ FACES_HD RowPlan make_row_plan(const FieldDesc &f, int chunk, int tiles_per_bloc
   return p;
 }
 
+// A tile whose rows are all local, with its x-lower end in the same column and
+// no x-upper end: not the first or last chunk of its column, not the first or
+// a virtual top row of elements in y or z.  The periodic step handles these
+// tiles of any field exactly as the general step does.
+FACES_HD bool interior_tile(const FieldDesc &f, int nchunks, int c, int jy, int jz)
+{
+  return c >= 1 && c < nchunks - 1 && jy >= 1 && jy < f.m[1] && jz >= 1 && jz < f.m[2];
+}
+
 struct TileCoords {
   int r, jy, jz, c;
   int jx0, jx1;

@@ -252,6 +252,76 @@ cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaS
   }
 }
 
+// The mixed tile step for fields the periodic step does not take (open
+// fields, v-26 messages): per tile, block-uniformly, interior tiles
+// (interior_tile) take the periodic step's staging and passes, the others
+// the general step's.  Shared memory holds both layouts' per-stage records.
+template <int N, int K, int NS>
+__global__ void __launch_bounds__(256, 3) mtile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int NN = N * N, NP = pieces_per_row(N);
+  constexpr int SPT = (NN * NP + 255) / 256;
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  double **lop_base = reinterpret_cast<double **>(sm + NS * stage);
+  unsigned *rfl_base = reinterpret_cast<unsigned *>(sm + NS * stage + lop_doubles(N, NS));
+  SlotCol *rinfo_base = reinterpret_cast<SlotCol *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS));
+  int4 *tinfo = reinterpret_cast<int4 *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS) +
+                                         rinfo_doubles(N, NS));
+  PMeta *meta = reinterpret_cast<PMeta *>(tinfo + NS);
+  TileWalk nw;
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;
+  ColKey ck{};
+  bool have_col = false;
+  SlotCol col[SPT];
+  // stage the next tile into stage st; the tile info's z: bit 0 hi_x, bit 1
+  // the periodic step
+  auto stage_next = [&](int st) {
+    if (interior_tile(f, p.nchunks, nw.u.c, nw.u.jy, nw.u.jz)) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + st * stage, meta + st, tinfo + st, threadIdx.x);
+      if (threadIdx.x == 0) tinfo[st].z = 2;
+    } else {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + st * stage, rfl_base + st * NN, lop_base + st * NN,
+                            rinfo_base + st * NN, tinfo + st);
+    }
+    walk_next(p, nw);
+    inflight++;
+  };
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) stage_next(j);
+    else cp_commit();
+  }
+  __syncthreads();
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    const unsigned *rfl = rfl_base + s * NN;
+    const int4 ti = tinfo[s];
+    const int nk = ti.y;
+    const bool hx = (ti.z & 1) != 0, lean = (ti.z & 2) != 0;
+    bool ok = true;
+    if (!lean && (int)threadIdx.x < NN) ok = row_regular(rfl[threadIdx.x], hx);
+    const int regular = __syncthreads_and(ok);
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) stage_next(sn);
+    else cp_commit();
+    double *buf = sm + s * stage;
+    if (nk > 0) {
+      if (lean) ptile::pxpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+      else sum_tile<N, K>(buf, rfl, nk, hx, regular != 0);
+    }
+    __syncthreads();
+    if (nk > 0) {
+      if (lean) ptile::pyzpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+      else store_tile<N, K, SPT>(buf, rfl, lop_base + s * NN, rinfo_base + s * NN, ti.x, nk, hx);
+    }
+    s = (s + 1) % NS;
+  }
+}
+
 bool tile_kernel_supported(int n) { return n >= 2 && n <= 12; }
 
 int tile_default_chunk(int n) { return tile_kmax(n); }
@@ -286,7 +356,17 @@ static cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
   static_assert(tile_stage_size<N, K>() * sizeof(double) % 16 == 0, "stage alignment");
   if (grid > p.ntiles) grid = p.ntiles;
   if (grid < 1) return cudaSuccess;
-  if (general || !ptile_field(f)) {
+  if (!general && !ptile_field(f)) {
+    const size_t smem = tile_smem_bytes(N, K) + sizeof(PMeta) * kTileStages;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(mtile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    mtile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  } else if (general) {
     const size_t smem = tile_smem_bytes(N, K);
     // the attribute is set once per process (one device per process)
     static bool configured = false;

@@ -50,9 +50,10 @@ extern "C" {
 #define FACES_GATHER 0x4u   /* force the generic one-thread-per-point kernel */
 #define FACES_ROWS 0x8u     /* use the register row kernel instead of the
                                shared-memory tile kernel */
-#define FACES_GENERAL 0x10u /* periodic direct-mode fields: use the general
-                               tile step instead of the periodic one (same
-                               result; for comparison) */
+#define FACES_GENERAL 0x10u /* use the general tile step everywhere instead of
+                               the periodic step (periodic direct-mode fields)
+                               or the mixed step (the others: periodic step
+                               on interior tiles); same result */
 #define FACES_V6 0x20u      /* v-6 strategy (gpu/v-6-messages-basic/Faces.cc:
                                65-173): six face messages per rank, sweeps z,
                                then y, then x; each point gets the tree sum in
@@ -128,17 +129,20 @@ int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int comput
 int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 
 /* Times the tile step on the field u over elements per tile (default, half,
- * double), units (half a column, one chunk) and resident blocks per SM
- * (default, 2), `trials` shares each after one warm-up, and keeps the
- * fastest (faces_set_tuning's settings).  Every timed launch is a share of
+ * double), units (half a column, one chunk, warp tiles) and resident blocks
+ * per SM (default, 2), and the general tile step and the row kernel at their
+ * defaults, `trials` shares each after one warm-up, and keeps the fastest
+ * (faces_set_tuning's settings and the kernel; faces_set_tuning returns to
+ * the tile step).  Every timed launch is a share of
  * u: returns how many it applied (>= 0; re-initialise u afterwards) or an
  * error code.  The reference fixes these choices at compile time
  * (MAXTHREADS, gpu/gpu.h:185-200).  Synchronous. */
 int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *stream);
 
 /* The tile step's current settings: elements per tile, x-chunks per unit
- * of work, blocks launched.  Any pointer may be NULL. */
-int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks);
+ * of work, blocks launched, and the kernel (0 the tile step, 1 the general
+ * tile step, 2 the row kernel).  Any pointer may be NULL. */
+int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel);
 
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);
