@@ -22,6 +22,9 @@
 //   --init=ref|int    initial state: gpu/main.cc:18 formula (default) or
 //                     integer values from --seed=S
 //   --chunk=K --tpb=T --order=O   work decomposition (faces_set_tuning)
+//   --autotune        pick the kernel and its settings on the field before the
+//                     timed loop (faces_autotune; the field is re-initialised
+//                     before each timed loop, as always)
 //   --json            one machine-readable line on stderr
 #include <cuda_runtime.h>
 
@@ -65,7 +68,7 @@ int main(int argc, char *argv[])
 {
   unsigned flags = 0;
   int init = 0, chunk = 0, tpb = 0, order = -1;
-  bool json = false;
+  bool json = false, autotune = false;
   unsigned long long seed = 1;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
@@ -76,6 +79,7 @@ int main(int argc, char *argv[])
     else if (s == "--v6") flags |= FACES_V6;
     else if (s == "--general") flags |= FACES_GENERAL;
     else if (s == "--json") json = true;
+    else if (s == "--autotune") autotune = true;
     else if (s == "--init=ref") init = 0;
     else if (s == "--init=int") init = 1;
     else if (s.rfind("--seed=", 0) == 0) seed = std::strtoull(s.c_str() + 7, nullptr, 10);
@@ -122,6 +126,11 @@ int main(int argc, char *argv[])
     faces_ctx *faces = nullptr;
     TRY(faces_create(&faces, lx, ly, lz, mx, my, mz, n, flags));
     if (chunk > 0 || tpb > 0 || order >= 0) TRY(faces_set_tuning(faces, chunk, tpb, order));
+    if (autotune) {
+      TRY(faces_init_int(faces, u, seed, nullptr));
+      const int applied = faces_autotune(faces, u, compute ? 1 : 0, 3, nullptr);
+      if (applied < 0) TRY(applied);
+    }
     std::cout << "Initialized Faces: " << mx << " x " << my << " x " << mz << " elements of order " << n - 1
               << " on " << lx << " x " << ly << " x " << lz << " tasks" << std::endl;
     for (int j = 0; j <= niel; j++) {
