@@ -54,7 +54,16 @@ E2E_SHARES = 100  # ni of the configuration (nk=1 nj=1 ni=100)
 # shares; here the re-init runs INSIDE the timed region and counts against
 # the result.
 RESEED_EVERY = 100
-KERNEL_BASE = "faces::ptile_kernel<8,{k},3>"  # the periodic tile step, n = 8, K elements per tile
+def kernel_name(t: dict) -> str:
+    """The step's kernel for n = 8 on this field from faces_get_tuning."""
+    k = 1 << max(0, (t["chunk"] - 1).bit_length())
+    if t["kernel"] == 2:
+        return "faces::rows_kernel<8>"
+    if t["kernel"] == 1:
+        return f"faces::tile_kernel<8,{k},3>"
+    if t["order"] == 3:
+        return "faces::wtile_kernel<8,1,3,4>"
+    return f"faces::ptile_kernel<8,{k},3>"
 L2_BYTES = 126 * 2 ** 20
 
 
@@ -227,9 +236,15 @@ def run_faces(args) -> dict | None:
     field_bytes = 8 * f.total_doubles
     u = f.field(dev)
     stream = torch.cuda.current_stream(dev)
-    # tile settings for this field, timed on the device (outside the timed region)
+    # tile settings for this field, timed on the device (outside the timed
+    # region), or given (--tune chunk,order,width: for profiling runs)
     f.init_int(u, SEED, stream)
-    f.autotune(u, True, 5, stream)
+    if args.tune:
+        f.set_tuning(*[int(x) for x in args.tune.split(",")])
+        how = f"given: --tune {args.tune}"
+    else:
+        f.autotune(u, True, 5, stream)
+        how = "faces_autotune before timing"
     tuned = f.tuning()
     f.init_int(u, SEED, stream)
     for _ in range(args.warmup):
@@ -309,12 +324,12 @@ def run_faces(args) -> dict | None:
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: integer-valued FP64 uniform in [0,2^20) (splitmix64 seed 1)",
-        "config": dict(workload_config(points, field_bytes), tuning=dict(tuned, how="faces_autotune before timing")),
+        "config": dict(workload_config(points, field_bytes), tuning=dict(tuned, how=how)),
         "pct_of_peak": round(100 * achieved / peak, 2),
         "points_per_s": round(world * points * args.steps / t_max, 1),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
-                     "kernel": KERNEL_BASE.format(k=1 << max(0, (tuned["chunk"] - 1).bit_length())),
+                     "kernel": kernel_name(tuned),
                      "algorithmic_bytes_per_launch": bytes_step,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
         "clocks": clocks,
@@ -523,6 +538,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--tune", default="", metavar="CHUNK,ORDER,WIDTH",
+                    help="set the tile settings instead of autotuning (profiling runs)")
     ap.add_argument("--profile-c4", type=int, default=0, metavar="N",
                     help="only build the 512-field batch and run N batched shares (for ncu)")
     args = ap.parse_args()

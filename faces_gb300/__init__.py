@@ -70,7 +70,7 @@ def lib() -> ctypes.CDLL:
     L.faces_launches_per_share.argtypes = [vp, c_int]
     L.faces_autotune.argtypes = [vp, dp, c_int, c_int, vp]
     L.faces_autotune.restype = c_int
-    L.faces_get_tuning.argtypes = [vp] + [ctypes.POINTER(c_int)] * 4
+    L.faces_get_tuning.argtypes = [vp] + [ctypes.POINTER(c_int)] * 5
     L.faces_get_tuning.restype = c_int
     L.faces_last_error.restype = ctypes.c_char_p
     ip = ctypes.POINTER(c_int)
@@ -308,9 +308,9 @@ class Faces:
     def tuning(self) -> dict:
         """The step's settings: elements per tile, chunks per unit, blocks, and
         the kernel (0 tile step, 1 general tile step, 2 row kernel)."""
-        v = [ctypes.c_int() for _ in range(4)]
+        v = [ctypes.c_int() for _ in range(5)]
         _check(lib().faces_get_tuning(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("chunk", "unit_chunks", "blocks", "kernel"), (x.value for x in v)))
+        return dict(zip(("chunk", "unit_chunks", "blocks", "kernel", "order"), (x.value for x in v)))
 
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))

@@ -241,10 +241,11 @@ int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
   return FACES_OK;
 }
 
-int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks, int *kernel)
+int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order)
 {
   if (int rc = check_ctx(c)) return rc;
   if (kernel) *kernel = c->variant;
+  if (order) *order = c->tplan.order;
   if (chunk) *chunk = c->tplan.chunk;
   if (unit_chunks) *unit_chunks = c->tplan.unit_chunks;
   if (blocks) *blocks = (int)c->tgrid;

@@ -140,9 +140,10 @@ int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *stream);
 
 /* The tile step's current settings: elements per tile, x-chunks per unit
- * of work, blocks launched, and the kernel (0 the tile step, 1 the general
- * tile step, 2 the row kernel).  Any pointer may be NULL. */
-int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel);
+ * of work, blocks launched, the kernel (0 the tile step, 1 the general tile
+ * step, 2 the row kernel) and the tile order (as faces_set_tuning; 3 warp
+ * tiles).  Any pointer may be NULL. */
+int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order);
 
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);

@@ -231,3 +231,17 @@ def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
         outs.append(u)
         f.close()
     assert torch.equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("args,opts", [("1 1 1 6 5 4 8 1 2 3", ["--periodic", "--init=int", "--autotune"]),
+                                       ("2 1 1 5 4 3 12 1 1 2", ["--autotune"]),
+                                       ("1 1 1 4 4 4 5 1 2 -5", ["--periodic", "--autotune"])])
+def test_executable_autotune(faces_lib, args, opts):
+    """The drop-in executable with --autotune still prints the reference's
+    pass line for every rank."""
+    import subprocess
+    exe = faces_lib.exe_path
+    r = subprocess.run([exe] + opts, input=args + "\n", capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    nranks = int(args.split()[0]) * int(args.split()[1]) * int(args.split()[2])
+    assert f"{nranks} tasks passed correctness check" in r.stdout, r.stdout
