@@ -240,7 +240,8 @@ def run_faces(args) -> dict | None:
     # region), or given (--tune chunk,order,width: for profiling runs)
     f.init_int(u, SEED, stream)
     if args.tune:
-        f.set_tuning(*[int(x) for x in args.tune.split(",")])
+        chunk, order, width = (int(x) for x in args.tune.split(","))
+        f.set_tuning(chunk=chunk, width=width, order=order)
         how = f"given: --tune {args.tune}"
     else:
         f.autotune(u, True, 5, stream)
