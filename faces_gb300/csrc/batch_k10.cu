@@ -1,0 +1,14 @@
+// batch_k10.cu -- the batched kernel's form MODE = 1, H = 0 (batch_impl.cuh).
+#include "batch_impl.cuh"
+
+namespace faces {
+
+cudaError_t batch_configure_10() { return batch_configure_t<1, 0>(); }
+
+cudaError_t batch_launch_10(const BatchField *fields, const BatchUnit *units, int nunits, long grid, int run,
+                            cudaStream_t s)
+{
+  return batch_launch_t<1, 0>(fields, units, nunits, grid, run, s);
+}
+
+}  // namespace faces

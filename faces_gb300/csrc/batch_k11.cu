@@ -1,0 +1,14 @@
+// batch_k11.cu -- the batched kernel's form MODE = 1, H = 1 (batch_impl.cuh).
+#include "batch_impl.cuh"
+
+namespace faces {
+
+cudaError_t batch_configure_11() { return batch_configure_t<1, 1>(); }
+
+cudaError_t batch_launch_11(const BatchField *fields, const BatchUnit *units, int nunits, long grid, int run,
+                            cudaStream_t s)
+{
+  return batch_launch_t<1, 1>(fields, units, nunits, grid, run, s);
+}
+
+}  // namespace faces

@@ -51,4 +51,18 @@ int batch_mode(const BatchField *fields, size_t n);
 cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int run,
                          int mode, int half, cudaStream_t s);
 
+// the kernel's forms, one translation unit each (batch_k<MODE><H>.cu):
+// MODE 0 general step, 1 periodic step, 2 each field its own; H the tile
+// length form (periodic step only)
+cudaError_t batch_configure_00();
+cudaError_t batch_configure_20();
+cudaError_t batch_configure_10();
+cudaError_t batch_configure_11();
+cudaError_t batch_configure_12();
+cudaError_t batch_launch_00(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+cudaError_t batch_launch_20(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+cudaError_t batch_launch_10(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+cudaError_t batch_launch_11(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+cudaError_t batch_launch_12(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+
 }  // namespace faces

@@ -1,0 +1,354 @@
+// tiles_impl.cuh -- the tile-step kernels and their per-n launchers
+// (templates).  Each tiles_n<N>.cu instantiates them for one n, so that the
+// build compiles the n's in parallel; tiles.cu holds the dispatch on n.
+//
+// Persistent CTAs walk the tiles of rows_setup.cuh.  Per tile: the staged
+// rows arrive by cp.async (three stages: the next two tiles' copies are in
+// flight while this one is summed), every owned shared point is summed once from
+// shared memory by one thread (tile_ops.cuh), and the changed rows are stored
+// back.  Global traffic is one read and one write of every row that holds a
+// shared point; the FP64 adds are dense in every warp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "geom.cuh"
+#include "kernels.cuh"
+#include "ptile_steps.cuh"
+#include "rows_setup.cuh"
+#include "tile_ops.cuh"
+#include "tile_steps.cuh"
+#include "tiles_dispatch.h"
+
+namespace faces {
+
+using namespace tiledev;
+
+
+template <int N, int K, int NS>
+__global__ void __launch_bounds__(256, 3) tile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int NN = N * N, NP = pieces_per_row(N), PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int SPT = (NN * NP + 255) / 256;
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
+  double **lop_base = reinterpret_cast<double **>(sm + NS * stage);
+  unsigned *rfl_base = reinterpret_cast<unsigned *>(sm + NS * stage + lop_doubles(N, NS));
+  SlotCol *rinfo_base = reinterpret_cast<SlotCol *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS));
+  int4 *tinfo = reinterpret_cast<int4 *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS) +
+                                         rinfo_doubles(N, NS));
+  static_assert(sizeof(SlotCol) == 16, "row info is two doubles");
+
+  // The block's tiles, walked by a TileWalk: a contiguous range (order 1),
+  // every gridDim.x-th tile (order 0), or every gridDim.x-th unit of
+  // unit_chunks consecutive chunks of one column, units ordered chunk group
+  // first so that the blocks running at one time hold neighbouring columns
+  // (order 2).  Consecutive tiles of one column share their rows' sources.
+  TileWalk nw;  // next tile to stage
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;  // staged tiles not yet summed
+  ColKey ck{};
+  bool have_col = false;
+  SlotCol col[SPT];  // the staged column's row sources, per owned slot
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + j * stage, rfl_base + j * NN, lop_base + j * NN,
+                            rinfo_base + j * NN, tinfo + j);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  // the loop reads row flags and tile infos other threads wrote
+  __syncthreads();
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    const unsigned *rfl = rfl_base + s * NN;
+    const int4 ti = tinfo[s];
+    const int nk = ti.y;
+    const bool hx = ti.z != 0;
+    bool ok = true;
+    if ((int)threadIdx.x < NN) ok = row_regular(rfl[threadIdx.x], hx);
+    const int regular = __syncthreads_and(ok);
+    // the stage of the previous tile is free again: the next prefetch goes there
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + sn * stage, rfl_base + sn * NN, lop_base + sn * NN,
+                            rinfo_base + sn * NN, tinfo + sn);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = sm + s * stage;
+    if (nk > 0) sum_tile<N, K>(buf, rfl, nk, hx, regular != 0);
+    __syncthreads();
+    if (nk > 0) store_tile<N, K, SPT>(buf, rfl, lop_base + s * NN, rinfo_base + s * NN, ti.x, nk, hx);
+    s = (s + 1) % NS;
+  }
+}
+
+// The periodic tile step (ptile_steps.cuh): the same pipeline with row
+// sources computed from four column offsets per tile.
+template <int N, int K, int NS>
+__global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
+  PMeta *meta = reinterpret_cast<PMeta *>(sm + NS * stage);
+  int4 *tinfo = reinterpret_cast<int4 *>(meta + NS);
+  TileWalk nw;
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j, threadIdx.x);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    // the staged tile, its infos, and the end of the previous tile's store
+    __syncthreads();
+    const int nk = tinfo[s].y;
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn, threadIdx.x);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = sm + s * stage;
+    ptile::pxpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+    __syncthreads();
+    ptile::pyzpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+    s = (s + 1) % NS;
+  }
+}
+
+// The warp-tile form of the periodic step: every warp stages, sums and
+// stores its own tiles (tile_kwarp(n) elements, wtile_stages(n) stages), so a
+// block holds kWarpsPerBlock independent pipelines and needs no block
+// barrier; warps walk the tiles chunk group first (tile q: chunk q / columns,
+// column q % columns) with a stride of all warps of the grid.
+template <int N, int K, int NS, int WPB>
+__global__ void __launch_bounds__(WPB * 32) wtile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *wsm = sm + (long)warp * NS * stage;
+  PMeta *meta_all = reinterpret_cast<PMeta *>(sm + (long)WPB * NS * stage);
+  PMeta *meta = meta_all + warp * NS;
+  int4 *tinfo = reinterpret_cast<int4 *>(meta_all + WPB * NS) + warp * NS;
+  const int ncol = (int)(p.ntiles / p.nchunks), total = (int)p.ntiles;
+  const int stride = gridDim.x * WPB;
+  int q = blockIdx.x * WPB + warp;  // next tile to stage
+  auto cursor = [&](int t) {
+    TileCursor u;
+    u.c = t / ncol;
+    const int col = t - u.c * ncol, t2 = col / p.ty;
+    u.jy = col - t2 * p.ty;
+    u.jz = t2 % p.tz;
+    u.r = t2 / p.tz;
+    return u;
+  };
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (q < total) {
+      ptile::pstage<N, K, 32>(f, p, cursor(q), wsm + j * stage, meta + j, tinfo + j, lane);
+      q += stride;
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    // the staged tile and its infos, and the end of the previous tile's work
+    __syncwarp();
+    const int nk = tinfo[s].y;
+    const int sn = (s + NS - 1) % NS;
+    if (q < total) {
+      ptile::pstage<N, K, 32>(f, p, cursor(q), wsm + sn * stage, meta + sn, tinfo + sn, lane);
+      q += stride;
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = wsm + s * stage;
+    ptile::pxpass<N, K, 32>(f.u, buf, meta + s, nk, lane);
+    __syncwarp();
+    ptile::pyzpass<N, K, 32>(f.u, buf, meta + s, nk, lane);
+    s = (s + 1) % NS;
+  }
+}
+
+// The mixed tile step for fields the periodic step does not take (open
+// fields, v-26 messages): per tile, block-uniformly, interior tiles
+// (interior_tile) take the periodic step's staging and passes, the others
+// the general step's.  Shared memory holds both layouts' per-stage records.
+template <int N, int K, int NS>
+__global__ void __launch_bounds__(256, 3) mtile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int NN = N * N, NP = pieces_per_row(N);
+  constexpr int SPT = (NN * NP + 255) / 256;
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  double **lop_base = reinterpret_cast<double **>(sm + NS * stage);
+  unsigned *rfl_base = reinterpret_cast<unsigned *>(sm + NS * stage + lop_doubles(N, NS));
+  SlotCol *rinfo_base = reinterpret_cast<SlotCol *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS));
+  int4 *tinfo = reinterpret_cast<int4 *>(sm + NS * stage + lop_doubles(N, NS) + rfl_doubles(N, NS) +
+                                         rinfo_doubles(N, NS));
+  PMeta *meta = reinterpret_cast<PMeta *>(tinfo + NS);
+  TileWalk nw;
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;
+  ColKey ck{};
+  bool have_col = false;
+  SlotCol col[SPT];
+  // stage the next tile into stage st; the tile info's z: bit 0 hi_x, bit 1
+  // the periodic step
+  auto stage_next = [&](int st) {
+    if (interior_tile(f, p.nchunks, nw.u.c, nw.u.jy, nw.u.jz)) {
+      ptile::pstage<N, K>(f, p, nw.u, sm + st * stage, meta + st, tinfo + st, threadIdx.x);
+      if (threadIdx.x == 0) tinfo[st].z = 2;
+    } else {
+      stage_tile<N, K, SPT>(f, p, nw.u, ck, have_col, col, sm + st * stage, rfl_base + st * NN, lop_base + st * NN,
+                            rinfo_base + st * NN, tinfo + st);
+    }
+    walk_next(p, nw);
+    inflight++;
+  };
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) stage_next(j);
+    else cp_commit();
+  }
+  __syncthreads();
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    const unsigned *rfl = rfl_base + s * NN;
+    const int4 ti = tinfo[s];
+    const int nk = ti.y;
+    const bool hx = (ti.z & 1) != 0, lean = (ti.z & 2) != 0;
+    bool ok = true;
+    if (!lean && (int)threadIdx.x < NN) ok = row_regular(rfl[threadIdx.x], hx);
+    const int regular = __syncthreads_and(ok);
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) stage_next(sn);
+    else cp_commit();
+    double *buf = sm + s * stage;
+    if (nk > 0) {
+      if (lean) ptile::pxpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+      else sum_tile<N, K>(buf, rfl, nk, hx, regular != 0);
+    }
+    __syncthreads();
+    if (nk > 0) {
+      if (lean) ptile::pyzpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+      else store_tile<N, K, SPT>(buf, rfl, lop_base + s * NN, rinfo_base + s * NN, ti.x, nk, hx);
+    }
+    s = (s + 1) % NS;
+  }
+}
+
+template <int N>
+inline cudaError_t launch_wtiles_n(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+{
+  constexpr int K = tile_kwarp(N);
+  if (p.chunk > K) return cudaErrorInvalidValue;
+  const size_t smem = wtile_smem_bytes(N);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  long blocks = (p.ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (grid < blocks) blocks = grid;
+  if (blocks < 1) return cudaSuccess;
+  wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock><<<(unsigned)blocks, 32 * kWarpsPerBlock, smem, s>>>(f, p);
+  return cudaGetLastError();
+}
+
+template <int N, int K>
+inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+{
+  static_assert(tile_stage_size<N, K>() * sizeof(double) % 16 == 0, "stage alignment");
+  if (grid > p.ntiles) grid = p.ntiles;
+  if (grid < 1) return cudaSuccess;
+  if (!general && !ptile_field(f)) {
+    const size_t smem = tile_smem_bytes(N, K) + sizeof(PMeta) * kTileStages;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(mtile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    mtile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  } else if (general) {
+    const size_t smem = tile_smem_bytes(N, K);
+    // the attribute is set once per process (one device per process)
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(tile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    tile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  } else {
+    const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() +
+                        (sizeof(PMeta) + sizeof(int4)) * kTileStages;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(ptile_kernel<N, K, kTileStages>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    ptile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
+  }
+  return cudaGetLastError();
+}
+
+template <int N>
+inline cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+{
+  constexpr int KM = tile_kinst_max(N);
+  if (p.chunk > KM) return cudaErrorInvalidValue;
+  switch (tile_instance_k(p.chunk)) {
+    case 1: return launch_tiles_nk<N, 1>(f, p, grid, general, s);
+    case 2: return launch_tiles_nk<N, 2>(f, p, grid, general, s);
+    case 4: return launch_tiles_nk<N, 4>(f, p, grid, general, s);
+    case 8: return launch_tiles_nk<N, 8>(f, p, grid, general, s);
+    case 16:
+      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, general, s);
+      return cudaErrorInvalidValue;
+    case 32:
+      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, general, s);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace faces

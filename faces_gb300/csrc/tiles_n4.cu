@@ -1,0 +1,16 @@
+// tiles_n4.cu -- the tile-step kernels for n = 4 (tiles_impl.cuh).
+#include "tiles_impl.cuh"
+
+namespace faces {
+
+cudaError_t tiles_n4(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+{
+  return launch_tiles_n<4>(f, p, grid, general, s);
+}
+
+cudaError_t wtiles_n4(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)
+{
+  return launch_wtiles_n<4>(f, p, grid, s);
+}
+
+}  // namespace faces
