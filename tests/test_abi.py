@@ -78,3 +78,26 @@ def test_struct_layouts_match_header(faces_lib, tmp_path):
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == [ctypes.sizeof(F.FacesJob), F.FacesJob.seed.offset, F.FacesJob.host_in.offset,
                    ctypes.sizeof(F.ServeStats), F.ServeStats.point_shares.offset, F.ServeStats.queued.offset]
+
+
+def test_batch_and_server_errors_without_gpu(faces_lib):
+    """Without a GPU, creating a batch or a server fails with FACES_ECUDA and a
+    message; NULL handles are rejected or accepted as documented."""
+    F = faces_lib
+    L = F.lib()
+    h = ctypes.c_void_p()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    assert L.faces_batch_create(ctypes.byref(h)) == -2 and L.faces_last_error()
+    assert L.faces_server_create(ctypes.byref(h), 1 << 30, 0, 0) == -2 and L.faces_last_error()
+    assert L.faces_server_create(ctypes.byref(h), 0, 0, 0) == -1
+    assert L.faces_batch_commit(None) == -1
+    assert L.faces_batch_destroy(None) == 0
+    assert L.faces_server_destroy(None) == 0
+    assert L.faces_server_poll(None, 0) == -1
+    with pytest.raises(F.FacesError):
+        F.Server(1 << 30)
