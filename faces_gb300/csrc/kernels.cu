@@ -102,29 +102,59 @@ __global__ void init_int_kernel(FieldDesc f, long total, unsigned long long seed
 // pack: the 26 messages of every rank, raw values before any sum
 // ---------------------------------------------------------------------------
 
-__global__ void pack_kernel(FieldDesc f)
+// Directions in launch order: the six faces, then the twelve edges and the
+// eight corners.
+__constant__ int kPackDirs[26] = {4,  10, 12, 14, 16, 22, 1,  3,  5,  7,  9,  11, 15,
+                                  17, 19, 21, 23, 25, 0,  2,  6,  8,  18, 20, 24, 26};
+
+// One block row per (rank, direction) of one group (faces: first = 0, count =
+// 6; edges and corners: first = 6, count = 20); threads stride over the
+// message.  The free axes' coordinates come from I-typed (32-bit where the
+// message allows) divisions, and the source offset from per-axis strides set
+// up once per block, so the per-point work is two or three divisions and one
+// load.
+template <typename I>
+__global__ void pack_kernel(FieldDesc f, int first, int count)
 {
-  const int rd = blockIdx.y;  // rank*27 + dir
-  const int r = rd / 27, dir = rd % 27;
-  if (dir == 13 || f.msg_off[rd] < 0) return;
+  const int r = blockIdx.y / count, dir = kPackDirs[first + blockIdx.y % count];
+  const int rd = r * 27 + dir;
+  if (f.msg_off[rd] < 0) return;
   const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
-  const long sz = region_size(f, d);
+  const long n = f.n;
+  // fixed axes: the boundary row of the boundary element; free axes in
+  // ascending order, the message's i-then-j position order (region_pos).
+  // Scalars, not arrays indexed by axis, so that nothing goes to local memory.
+  long base = (long)r * f.R, si0 = 0, sj0 = 0, si1 = 0, sj1 = 0;
+  int nfree = 0, m0 = 1;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const long sia = a == 0 ? 1 : a == 1 ? n : n * n;
+    const long sja = a == 0 ? n * n * n : a == 1 ? f.sjy : f.sjz;
+    if (d[a] == 0) {
+      if (nfree == 0) { si0 = sia; sj0 = sja; m0 = f.m[a]; }
+      else { si1 = sia; sj1 = sja; }
+      nfree++;
+    } else if (d[a] > 0) {
+      base += (n - 1) * sia + (long)(f.m[a] - 1) * sja;
+    }
+  }
+  const I sz = (I)region_size(f, d);
   double *out = f.msg + f.msg_off[rd];
-  const double *ur = f.u + (long)r * f.R;
-  const int n = f.n;
-  for (long pos = blockIdx.x * (long)blockDim.x + threadIdx.x; pos < sz; pos += (long)gridDim.x * blockDim.x) {
-    int i[3], j[3];
-    long t = pos;
-    for (int a = 0; a < 3; a++)
-      if (d[a] == 0) { i[a] = (int)(t % n); t /= n; }
-    for (int a = 0; a < 3; a++)
-      if (d[a] == 0) { j[a] = (int)(t % f.m[a]); t /= f.m[a]; }
-    for (int a = 0; a < 3; a++)
-      if (d[a] != 0) {
-        i[a] = d[a] < 0 ? 0 : n - 1;
-        j[a] = d[a] < 0 ? 0 : f.m[a] - 1;
+  const double *ur = f.u + base;
+  const I nn = (I)(nfree == 2 ? n * n : n), nI = (I)n, mI = (I)m0;
+  for (I pos = blockIdx.x * (I)blockDim.x + threadIdx.x; pos < sz; pos += (I)gridDim.x * blockDim.x) {
+    long src;
+    if (nfree == 0) {
+      src = 0;
+    } else {
+      const I q = pos % nn, e = pos / nn;
+      if (nfree == 1) {
+        src = (long)q * si0 + (long)e * sj0;
+      } else {
+        src = (long)(q % nI) * si0 + (long)(q / nI) * si1 + (long)(e % mI) * sj0 + (long)(e / mI) * sj1;
       }
-    out[pos] = ur[elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+    }
+    out[pos] = ur[src];
   }
 }
 
@@ -135,16 +165,17 @@ __global__ void pack_kernel(FieldDesc f)
 // Rank-local point coordinate g in [0, m*(n-1)] along one axis: element E
 // holds g = E*(n-1)+i.  A point with g % (n-1) == 0 has a lower copy (E-1,
 // n-1) and an upper copy (E, 0); elements -1 and m belong to the neighbours.
+// Scalars (and loops unrolled over fixed bounds below), so that no array is
+// indexed at run time and nothing goes to local memory.
 struct Copies {
-  int cnt;
-  int e[2], i[2];
+  int cnt, e0, i0, e1, i1;
 };
 
-__device__ __forceinline__ void local_axis(int g, int n, Copies &c)
+__device__ __forceinline__ Copies local_axis(int g, int n)
 {
   const int nm1 = n - 1, E = g / nm1, i = g % nm1;
-  if (i) { c.cnt = 1; c.e[0] = E; c.i[0] = i; return; }
-  c.cnt = 2; c.e[0] = E - 1; c.i[0] = nm1; c.e[1] = E; c.i[1] = 0;
+  if (i) return Copies{1, E, i, E, i};
+  return Copies{2, E - 1, nm1, E, 0};
 }
 
 // One shared point: point g (global in rank r's subdomain) and its copies,
@@ -157,36 +188,41 @@ __device__ __forceinline__ void gather_point(const FieldDesc &f, int r, const in
   if (g[0] % nm1 && g[1] % nm1 && g[2] % nm1) return;
   bool onb = false, skip = false;
   Copies c[3];
+#pragma unroll
   for (int a = 0; a < 3; a++) {
     const int Ga = f.m[a] * nm1;
     onb |= (g[a] == 0 || g[a] == Ga);
-    int up[3] = {0, 0, 0};
-    up[a] = 1;
     // direct mode: the upper rank owns the points of the shared plane
-    if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(up[0], up[1], up[2])) >= 0) skip = true;
-    local_axis(g[a], n, c[a]);
+    if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(a == 0, a == 1, a == 2)) >= 0) skip = true;
+    Copies x = local_axis(g[a], n);
     // drop copies whose neighbour rank does not exist
-    int k = 0;
-    for (int b = 0; b < c[a].cnt; b++) {
-      const int e = c[a].e[b];
-      int dv[3] = {0, 0, 0};
-      dv[a] = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
-      if (dv[a] && nbr_of(f, r, dir_index(dv[0], dv[1], dv[2])) < 0) continue;
-      c[a].e[k] = e; c[a].i[k] = c[a].i[b]; k++;
-    }
-    c[a].cnt = k;
+    auto exists = [&](int e) {
+      const int dv = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
+      return dv == 0 || nbr_of(f, r, dir_index(a == 0 ? dv : 0, a == 1 ? dv : 0, a == 2 ? dv : 0)) >= 0;
+    };
+    const bool ok0 = exists(x.e0), ok1 = x.cnt == 2 && exists(x.e1);
+    if (!ok0) { x.e0 = x.e1; x.i0 = x.i1; }
+    x.cnt = (int)ok0 + (int)ok1;
+    c[a] = x;
   }
   if (skip) return;
   if (c[0].cnt * c[1].cnt * c[2].cnt < 2) return;
   if (!compute && !onb) return;
   double v[2][2][2];
   double *w[2][2][2];
-  for (int bz = 0; bz < c[2].cnt; bz++)
-    for (int by = 0; by < c[1].cnt; by++)
-      for (int bx = 0; bx < c[0].cnt; bx++) {
-        int e[3] = {c[0].e[bx], c[1].e[by], c[2].e[bz]};
-        const int i[3] = {c[0].i[bx], c[1].i[by], c[2].i[bz]};
+#pragma unroll
+  for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+    for (int by = 0; by < 2; by++)
+#pragma unroll
+      for (int bx = 0; bx < 2; bx++) {
+        w[bz][by][bx] = nullptr;
+        v[bz][by][bx] = 0.0;
+        if (bz >= c[2].cnt || by >= c[1].cnt || bx >= c[0].cnt) continue;
+        const int e[3] = {bx ? c[0].e1 : c[0].e0, by ? c[1].e1 : c[1].e0, bz ? c[2].e1 : c[2].e0};
+        const int i[3] = {bx ? c[0].i1 : c[0].i0, by ? c[1].i1 : c[1].i0, bz ? c[2].i1 : c[2].i0};
         int d[3], j[3];
+#pragma unroll
         for (int a = 0; a < 3; a++) {
           d[a] = e[a] < 0 ? -1 : (e[a] >= f.m[a] ? 1 : 0);
           j[a] = e[a] < 0 ? f.m[a] - 1 : (e[a] >= f.m[a] ? 0 : e[a]);
@@ -199,20 +235,24 @@ __device__ __forceinline__ void gather_point(const FieldDesc &f, int r, const in
           v[bz][by][bx] = *ptr;
         } else {
           const double *rb = recv_of(f, r, dir);
-          w[bz][by][bx] = nullptr;
           v[bz][by][bx] = rb[region_pos(f, d, i, j)];
         }
       }
   double sy[2];
-  for (int bz = 0; bz < c[2].cnt; bz++) {
+#pragma unroll
+  for (int bz = 0; bz < 2; bz++) {
     double sx[2];
-    for (int by = 0; by < c[1].cnt; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
+#pragma unroll
+    for (int by = 0; by < 2; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
     sy[bz] = (c[1].cnt == 2) ? sx[0] + sx[1] : sx[0];
   }
   const double s = (c[2].cnt == 2) ? sy[0] + sy[1] : sy[0];
-  for (int bz = 0; bz < c[2].cnt; bz++)
-    for (int by = 0; by < c[1].cnt; by++)
-      for (int bx = 0; bx < c[0].cnt; bx++)
+#pragma unroll
+  for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+    for (int by = 0; by < 2; by++)
+#pragma unroll
+      for (int bx = 0; bx < 2; bx++)
         if (w[bz][by][bx]) *w[bz][by][bx] = s;
 }
 
@@ -597,18 +637,33 @@ cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStr
 // faces, low then high.
 // ---------------------------------------------------------------------------
 
+// Dimension d's sweep: a and b are the other two axes (a < b); sp* and se*
+// are the point and element strides of each axis, set on the host so that the
+// kernels index no array by a run-time axis (that would put it in local
+// memory).
 struct V6Geom {
-  int d, a, b;
+  int d, n, ma, mb, md;
   long F, per_rank, off;  // face doubles, doubles per rank, offset of dimension d
+  long spa, spb, spd, sea, seb, sed;
 };
 
 V6Geom v6_geom(const FieldDesc &f, int d)
 {
   V6Geom g;
   g.d = d;
-  g.a = d == 0 ? 1 : 0;
-  g.b = d == 2 ? 1 : 2;
-  const long nn = (long)f.n * f.n;
+  g.n = f.n;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  const long n = f.n, nn = n * n;
+  const long sp[3] = {1, n, nn}, se[3] = {nn * n, f.sjy, f.sjz};
+  g.ma = f.m[a];
+  g.mb = f.m[b];
+  g.md = f.m[d];
+  g.spa = sp[a];
+  g.spb = sp[b];
+  g.spd = sp[d];
+  g.sea = se[a];
+  g.seb = se[b];
+  g.sed = se[d];
   const long Fd[3] = {nn * f.m[1] * f.m[2], nn * f.m[0] * f.m[2], nn * f.m[0] * f.m[1]};
   g.F = Fd[d];
   g.per_rank = 2 * (Fd[0] + Fd[1] + Fd[2]);
@@ -618,78 +673,80 @@ V6Geom v6_geom(const FieldDesc &f, int d)
 
 long v6_message_doubles(const FieldDesc &f) { return v6_geom(f, 0).per_rank * f.nranks; }
 
-__device__ __forceinline__ void v6_point(const FieldDesc &f, const V6Geom &g, long idx, int i[3], int j[3])
+// face point idx of a dimension-d face: (ia, ib) fastest, then ja, then jb
+struct V6Point {
+  int ia, ib, ja, jb;
+  long off;  // ia*spa + ib*spb + ja*sea + jb*seb
+};
+
+template <typename I>
+__device__ __forceinline__ V6Point v6_point(const V6Geom &g, I idx)
 {
-  const int n = f.n;
-  const long nn = (long)n * n, pa = nn * f.m[g.a];
-  const int jb = (int)(idx / pa);
-  long q = idx - (long)jb * pa;
-  const int ja = (int)(q / nn);
-  q -= (long)ja * nn;
-  i[g.b] = (int)(q / n);
-  i[g.a] = (int)(q - (long)i[g.b] * n);
-  j[g.a] = ja;
-  j[g.b] = jb;
+  const I n = (I)g.n, nn = n * n, pa = nn * (I)g.ma;
+  V6Point p;
+  const I jb = idx / pa;
+  I q = idx - jb * pa;
+  const I ja = q / nn;
+  q -= ja * nn;
+  const I ib = q / n;
+  p.ia = (int)(q - ib * n);
+  p.ib = (int)ib;
+  p.ja = (int)ja;
+  p.jb = (int)jb;
+  p.off = p.ia * g.spa + p.ib * g.spb + p.ja * g.sea + p.jb * g.seb;
+  return p;
 }
 
 // every rank's two faces of dimension d, after the earlier sweeps
+template <typename I>
 __global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
 {
-  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= f.nranks * 2 * g.F) return;
-  const int r = (int)(t / (2 * g.F));
-  const long rem = t - (long)r * 2 * g.F;
-  const int side = rem >= g.F;
-  const long idx = rem - side * g.F;
-  int i[3], j[3];
-  v6_point(f, g, idx, i, j);
-  i[g.d] = side ? f.n - 1 : 0;
-  j[g.d] = side ? f.m[g.d] - 1 : 0;
-  msg[(long)r * g.per_rank + g.off + side * g.F + idx] =
-      f.u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
+  const I F2 = 2 * (I)g.F;
+  if (t >= (I)f.nranks * F2) return;
+  const I r = t / F2;
+  const I rem = t - r * F2;
+  const int side = rem >= (I)g.F;
+  const I idx = rem - (side ? (I)g.F : 0);
+  const V6Point p = v6_point(g, idx);
+  const long hi_off = side ? (long)(g.n - 1) * g.spd + (long)(g.md - 1) * g.sed : 0;
+  msg[(long)r * g.per_rank + g.off + (side ? g.F : 0) + (long)idx] = f.u[(long)r * f.R + p.off + hi_off];
 }
 
 // low face += the lower neighbour's high face, element pairs along d, high
 // face += the upper neighbour's low face; compute = 0: element pairs only
 // where the point is on the subdomain boundary in another dimension
+template <typename I>
 __global__ void v6_update_kernel(FieldDesc f, V6Geom g, const double *msg, int compute)
 {
-  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (t >= f.nranks * g.F) return;
-  const int r = (int)(t / g.F);
-  const long idx = t - (long)r * g.F;
-  const int n = f.n, d = g.d;
-  int i[3], j[3];
-  v6_point(f, g, idx, i, j);
-  const bool on_a = (i[g.a] == 0 && j[g.a] == 0) || (i[g.a] == n - 1 && j[g.a] == f.m[g.a] - 1);
-  const bool on_b = (i[g.b] == 0 && j[g.b] == 0) || (i[g.b] == n - 1 && j[g.b] == f.m[g.b] - 1);
-  const int dm[3] = {d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0};
-  const int lo = nbr_of(f, r, dir_index(dm[0], dm[1], dm[2]));
-  const int hi = nbr_of(f, r, dir_index(-dm[0], -dm[1], -dm[2]));
-  double *ur = f.u + (long)r * f.R;
-  i[d] = 0;
-  j[d] = 0;
+  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
+  if (t >= (I)f.nranks * (I)g.F) return;
+  const I r = t / (I)g.F;
+  const I idx = t - r * (I)g.F;
+  const int n = g.n, d = g.d;
+  const V6Point pt = v6_point(g, idx);
+  const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
+  const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
+  const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
+  const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
+  double *ur = f.u + (long)r * f.R + pt.off;
+  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
   if (lo >= 0) {
-    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
-    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + idx];
+    double *p = ur;
+    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + (long)idx];
   }
   if (compute || on_a || on_b) {
-    const long sd = d == 0 ? (long)n * n * n : d == 1 ? f.sjy : f.sjz;  // element stride along d
-    const long pd = d == 0 ? 1 : d == 1 ? n : (long)n * n;              // point stride along d
-    i[d] = n - 1;
-    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
-    for (int jd = 0; jd + 1 < f.m[d]; jd++, p += sd) {
-      double *q = p + sd - (long)(n - 1) * pd;
+    double *p = ur + top;
+    for (int jd = 0; jd + 1 < g.md; jd++, p += g.sed) {
+      double *q = p + g.sed - top;
       const double v = *p + *q;
       *p = v;
       *q = v;
     }
   }
   if (hi >= 0) {
-    i[d] = n - 1;
-    j[d] = f.m[d] - 1;
-    double *p = ur + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
-    *p = *p + msg[(long)hi * g.per_rank + g.off + idx];
+    double *p = ur + top + (long)(g.md - 1) * g.sed;
+    *p = *p + msg[(long)hi * g.per_rank + g.off + (long)idx];
   }
 }
 
@@ -698,25 +755,42 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
   for (int d = 2; d >= 0; d--) {
     const V6Geom g = v6_geom(f, d);
     const long np = f.nranks * 2 * g.F, nu = f.nranks * g.F;
-    v6_pack_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
-    v6_update_kernel<<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
+    // 32-bit index math while every thread index (and the next block's) fits
+    if (np + 256 < (1L << 31)) {
+      v6_pack_kernel<unsigned><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+      v6_update_kernel<unsigned><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
+    } else {
+      v6_pack_kernel<unsigned long><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+      v6_update_kernel<unsigned long><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
+    }
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
 {
-  long maxsz = 0;
+  // faces, then edges and corners: each group's grid is sized for its own
+  // largest message, so that few blocks find nothing to do; blocks stride so
+  // that the faces take about two waves of 8 blocks per SM
   const int dface[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const int dedge[3][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}};
+  long face = 0, edge = 1;
   for (int a = 0; a < 3; a++) {
-    const long sz = region_size(f, dface[a]);
-    if (sz > maxsz) maxsz = sz;
+    face = face > region_size(f, dface[a]) ? face : region_size(f, dface[a]);
+    edge = edge > region_size(f, dedge[a]) ? edge : region_size(f, dedge[a]);
   }
-  long bx = (maxsz + 255) / 256;
-  if (bx > 4096) bx = 4096;
-  if (bx < 1) bx = 1;
-  dim3 grid((unsigned)bx, (unsigned)(f.nranks * 27));
-  pack_kernel<<<grid, 256, 0, s>>>(f);
+  const long per_wave = 152L * 8 * 2;
+  const long groups[2][3] = {{0, 6, face}, {6, 20, edge}};
+  for (const auto &g : groups) {
+    const long rows = (long)f.nranks * g[1];
+    long bx = (g[2] + 255) / 256;
+    const long want = (per_wave + rows - 1) / rows;
+    if (bx > want) bx = want;
+    if (bx < 1) bx = 1;
+    dim3 grid((unsigned)bx, (unsigned)rows);
+    if (g[2] + 256L * bx < (1L << 31)) pack_kernel<unsigned><<<grid, 256, 0, s>>>(f, (int)g[0], (int)g[1]);
+    else pack_kernel<unsigned long><<<grid, 256, 0, s>>>(f, (int)g[0], (int)g[1]);
+  }
   return cudaGetLastError();
 }
 
