@@ -107,16 +107,31 @@ __global__ void init_int_kernel(FieldDesc f, long total, unsigned long long seed
 __constant__ int kPackDirs[26] = {4,  10, 12, 14, 16, 22, 1,  3,  5,  7,  9,  11, 15,
                                   17, 19, 21, 23, 25, 0,  2,  6,  8,  18, 20, 24, 26};
 
-// One block row per (rank, direction) of one group (faces: first = 0, count =
-// 6; edges and corners: first = 6, count = 20); threads stride over the
-// message.  The free axes' coordinates come from I-typed (32-bit where the
-// message allows) divisions, and the source offset from per-axis strides set
-// up once per block, so the per-point work is two or three divisions and one
-// load.
+// Block rows 0 .. nranks*6-1: one face message each (rank, face), the row's
+// blocks striding over it.  Blocks beyond: one edge or corner message each
+// (nranks*20 of them, numbered across the remaining rows).  The free axes'
+// coordinates come from I-typed (32-bit where the message allows) divisions,
+// and the source offset from per-axis strides set up once per block, so the
+// per-point work is two or three divisions and one load.
 template <typename I>
-__global__ void pack_kernel(FieldDesc f, int first, int count)
+__global__ void pack_kernel(FieldDesc f)
 {
-  const int r = blockIdx.y / count, dir = kPackDirs[first + blockIdx.y % count];
+  const int face_rows = f.nranks * 6;
+  int r, dir;
+  I part, parts;
+  if ((int)blockIdx.y < face_rows) {
+    r = blockIdx.y / 6;
+    dir = kPackDirs[blockIdx.y % 6];
+    part = blockIdx.x;
+    parts = gridDim.x;
+  } else {
+    const int e = ((int)blockIdx.y - face_rows) * (int)gridDim.x + (int)blockIdx.x;
+    if (e >= f.nranks * 20) return;
+    r = e / 20;
+    dir = kPackDirs[6 + e % 20];
+    part = 0;
+    parts = 1;
+  }
   const int rd = r * 27 + dir;
   if (f.msg_off[rd] < 0) return;
   const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
@@ -142,7 +157,7 @@ __global__ void pack_kernel(FieldDesc f, int first, int count)
   double *out = f.msg + f.msg_off[rd];
   const double *ur = f.u + base;
   const I nn = (I)(nfree == 2 ? n * n : n), nI = (I)n, mI = (I)m0;
-  for (I pos = blockIdx.x * (I)blockDim.x + threadIdx.x; pos < sz; pos += (I)gridDim.x * blockDim.x) {
+  for (I pos = part * (I)blockDim.x + threadIdx.x; pos < sz; pos += parts * (I)blockDim.x) {
     long src;
     if (nfree == 0) {
       src = 0;
@@ -769,9 +784,8 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
 
 cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
 {
-  // faces, then edges and corners: each group's grid is sized for its own
-  // largest message, so that few blocks find nothing to do; blocks stride so
-  // that the faces take about two waves of 8 blocks per SM
+  // face rows strided by about two waves of 8 blocks per SM, then one block
+  // per edge or corner message, in one launch
   const int dface[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
   const int dedge[3][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}};
   long face = 0, edge = 1;
@@ -779,18 +793,14 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
     face = face > region_size(f, dface[a]) ? face : region_size(f, dface[a]);
     edge = edge > region_size(f, dedge[a]) ? edge : region_size(f, dedge[a]);
   }
-  const long per_wave = 152L * 8 * 2;
-  const long groups[2][3] = {{0, 6, face}, {6, 20, edge}};
-  for (const auto &g : groups) {
-    const long rows = (long)f.nranks * g[1];
-    long bx = (g[2] + 255) / 256;
-    const long want = (per_wave + rows - 1) / rows;
-    if (bx > want) bx = want;
-    if (bx < 1) bx = 1;
-    dim3 grid((unsigned)bx, (unsigned)rows);
-    if (g[2] + 256L * bx < (1L << 31)) pack_kernel<unsigned><<<grid, 256, 0, s>>>(f, (int)g[0], (int)g[1]);
-    else pack_kernel<unsigned long><<<grid, 256, 0, s>>>(f, (int)g[0], (int)g[1]);
-  }
+  const long face_rows = (long)f.nranks * 6, small = (long)f.nranks * 20;
+  long bx = (face + 255) / 256;
+  const long want = (152L * 8 * 2 + face_rows - 1) / face_rows;
+  if (bx > want) bx = want;
+  if (bx < 1) bx = 1;
+  const dim3 grid((unsigned)bx, (unsigned)(face_rows + (small + bx - 1) / bx));
+  if (face + 256L * bx < (1L << 31) && edge < (1L << 30)) pack_kernel<unsigned><<<grid, 256, 0, s>>>(f);
+  else pack_kernel<unsigned long><<<grid, 256, 0, s>>>(f);
   return cudaGetLastError();
 }
 
