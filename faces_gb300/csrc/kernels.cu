@@ -89,12 +89,16 @@ __global__ void init_ref_kernel(FieldDesc f, long total)
   }
 }
 
-__global__ void init_int_kernel(FieldDesc f, long total, unsigned long long seed)
+// Block rows stride over the slabs (rank, jz) of sjz doubles each (R = mz *
+// sjz), threads over a slab's doubles: no division per element.
+__global__ void init_int_kernel(FieldDesc f, long slabs, unsigned long long seed)
 {
   const long plane = f.sjy * f.m[1];
-  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
-    const long q = (p % f.R) % f.sjz;
-    f.u[p] = (q < plane) ? int_value(seed, p) : 0.0;
+  for (long sl = blockIdx.y; sl < slabs; sl += gridDim.y) {
+    const long p0 = sl * f.sjz;
+    double *slab = f.u + p0;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < f.sjz; q += (long)gridDim.x * blockDim.x)
+      slab[q] = (q < plane) ? int_value(seed, p0 + q) : 0.0;
   }
 }
 
@@ -638,7 +642,13 @@ cudaError_t launch_init_ref(const FieldDesc &f, cudaStream_t s)
 
 cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStream_t s)
 {
-  init_int_kernel<<<152 * 8, 256, 0, s>>>(f, f.R * f.nranks, seed);
+  const long slabs = (long)f.nranks * f.m[2];
+  const long rows = slabs < 65535 ? slabs : 65535;
+  long bx = (f.sjz + 255) / 256;
+  const long want = (152L * 8 * 4 + rows - 1) / rows;
+  if (bx > want) bx = want;
+  if (bx < 1) bx = 1;
+  init_int_kernel<<<dim3((unsigned)bx, (unsigned)rows), 256, 0, s>>>(f, slabs, seed);
   return cudaGetLastError();
 }
 
