@@ -51,7 +51,7 @@ constexpr long batch_smem_bytes(int h)
 {
   return sizeof(double) * (long)kBatchStages * (h == 2 ? kStage<2> : h ? kStage<1> : kStage<0>) + sizeof(double *) * (long)kBatchStages * kNNMax +
          sizeof(SlotCol) * (long)kBatchStages * kNNMax + sizeof(unsigned) * (long)kBatchStages * kNNMax +
-         sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages + sizeof(BatchField);
+         sizeof(int4) * kBatchStages + sizeof(PMeta) * kBatchStages + 2 * sizeof(BatchField);
 }
 
 struct BWalk {
@@ -107,7 +107,7 @@ struct Smem {
   unsigned *rfl;
   int4 *tinfo;
   PMeta *meta;
-  BatchField *field;  // the block's copy of the field it stages
+  BatchField *field;  // two slots: the block's copies of the fields it stages
 };
 
 template <int H>
@@ -140,28 +140,30 @@ __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u
                                   m.rfl + st * kNNMax, m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
 }
 
-// stage tile u of field `field` into stage st; the tile info's z holds
-// hi_x | lean << 1 | n << 2 and w the field
-// copy field `field` to the block's shared copy.  Only on a change of field
-// (the same for every thread of the block): a barrier so that no thread still
-// reads the previous copy, the copy, a barrier so that every thread sees it.
-__device__ __forceinline__ void load_field(const BatchField *fields, int field, const Smem &m, int &cached)
+constexpr int kFieldWords = (int)(sizeof(BatchField) / 8);
+
+// copy field `field` into a shared slot, with a barrier on each side (the
+// prologue only: in the main loop the copy of the next tile's field is
+// loaded early and stored into the other slot before the loop's barrier).
+// Block-uniform: every thread sees the same field.
+__device__ __forceinline__ void load_field(const BatchField *fields, int field, BatchField *slot, int &cached)
 {
   if (field == cached) return;
   static_assert(sizeof(BatchField) % 8 == 0, "field table entries are whole words");
   const long long *src = reinterpret_cast<const long long *>(fields + field);
-  long long *dst = reinterpret_cast<long long *>(m.field);
+  long long *dst = reinterpret_cast<long long *>(slot);
   __syncthreads();
-  for (int i = threadIdx.x; i < (int)(sizeof(BatchField) / 8); i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < kFieldWords; i += blockDim.x) dst[i] = src[i];
   __syncthreads();
   cached = field;
 }
 
+// stage tile u of field `field` (its copy: bf) into stage st; the tile
+// info's z holds hi_x | lean << 1 | n << 2 and w the field
 template <int MODE, int H>
-__device__ __forceinline__ void bstage_any(int field, const TileCursor &u, ColKey &ck, bool &have_col,
-                                           SlotCol (&col)[kSptMax], const Smem &m, int st)
+__device__ __forceinline__ void bstage_any(int field, const BatchField &bf, const TileCursor &u, ColKey &ck,
+                                           bool &have_col, SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
-  const BatchField &bf = *m.field;
   switch (bf.f.n) {
 #define FACES_BSTAGE(NV) \
   case NV: bstage<NV, MODE, H>(bf, u, ck, have_col, col, m, st); break;
@@ -193,21 +195,25 @@ __global__ void __launch_bounds__(256, bblocks(H))
   bwalk_unit(fields, units, nw);
   ColKey ck{};
   bool have_col = false;
-  int last_field = -1, cached = -1;
+  int last_field = -1;
+  // field slots: the next tile to stage takes slot `cur` (holding field
+  // cached_cur); the other slot holds cached_oth
+  int cur = 0, cached_cur = -1, cached_oth = -1;
   SlotCol col[kSptMax];
   int inflight = 0;
 #pragma unroll
   for (int j = 0; j < kBatchStages - 1; j++) {
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      load_field(fields, nw.field, m, cached);
-      bstage_any<MODE, H>(nw.field, nw.cur, ck, have_col, col, m, j);
+      load_field(fields, nw.field, m.field + cur, cached_cur);
+      bstage_any<MODE, H>(nw.field, m.field[cur], nw.cur, ck, have_col, col, m, j);
       bwalk_next(fields, units, nunits, run, nw);
       inflight++;
     } else {
       cp_commit();
     }
   }
+  if (!nw.done) load_field(fields, nw.field, m.field + cur, cached_cur);
   __syncthreads();
   int s = 0;
   for (; inflight > 0; inflight--) {
@@ -222,10 +228,25 @@ __global__ void __launch_bounds__(256, bblocks(H))
     const int sn = (s + kBatchStages - 1) % kBatchStages;
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
-      load_field(fields, nw.field, m, cached);
-      bstage_any<MODE, H>(nw.field, nw.cur, ck, have_col, col, m, sn);
+      bstage_any<MODE, H>(nw.field, m.field[cur], nw.cur, ck, have_col, col, m, sn);
       bwalk_next(fields, units, nunits, run, nw);
       inflight++;
+      // the field of the tile staged next: already in a slot, or copied now
+      // into the other slot, which nobody reads in this iteration (its last
+      // readers staged before this iteration's barrier; the next iteration's
+      // barrier publishes the copy)
+      if (!nw.done && nw.field != cached_cur) {
+        if (nw.field != cached_oth) {
+          if ((int)threadIdx.x < kFieldWords)
+            reinterpret_cast<long long *>(m.field + (cur ^ 1))[threadIdx.x] =
+                reinterpret_cast<const long long *>(fields + nw.field)[threadIdx.x];
+          cached_oth = nw.field;
+        }
+        const int was = cached_cur;
+        cached_cur = cached_oth;
+        cached_oth = was;
+        cur ^= 1;
+      }
     } else {
       cp_commit();
     }
