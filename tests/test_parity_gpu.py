@@ -210,14 +210,15 @@ def test_warp_tiles_bit_exact(oracle, faces_lib, shape):
 
 
 @pytest.mark.parametrize("shape", [(1, 1, 1, 15, 14, 13, 12), (2, 2, 1, 9, 7, 5, 11), (1, 2, 2, 11, 6, 7, 10),
-                                   (3, 1, 1, 6, 9, 8, 9), (1, 1, 1, 24, 5, 6, 3)],
+                                   (3, 1, 1, 6, 9, 8, 9), (1, 1, 1, 24, 5, 6, 3), (3, 3, 3, 16, 16, 16, 6)],
                          ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
 @pytest.mark.parametrize("mode", ["tiles", "general", "rows", "messages", "v6"])
 def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
-    """The reference's 15x14x13 n=12 shape and other shapes with every
-    dimension several elements long, every strategy: the device closed form
-    after 3 shares, and equality with the default kernel bit for bit."""
+    """The reference's 15x14x13 n=12 shape, the 3x3x3-rank 16^3 n=6 grid at
+    full size, and other shapes with every dimension several elements long,
+    every strategy: the device closed form after 3 shares, and equality with
+    the default kernel bit for bit."""
     F = faces_lib
     outs = []
     for m in ("tiles", mode):
