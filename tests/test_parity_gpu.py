@@ -234,6 +234,28 @@ def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
     assert torch.equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("shape", [(1, 1, 1, 15, 14, 13, 12), (2, 2, 1, 9, 7, 5, 11), (3, 3, 3, 16, 16, 16, 6)],
+                         ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+@pytest.mark.parametrize("mode", ["messages", "v6", "gather"])
+def test_larger_shapes_without_compute(faces_lib, shape, periodic, mode):
+    """compute = 0 (the reference's ni < 0) on the larger shapes: the
+    boundary-only sums of every strategy against the device closed form, and
+    bit-equal to the default path."""
+    F = faces_lib
+    outs = []
+    for m in ("tiles", mode):
+        f = F.Faces(*shape, periodic=periodic, messages=m == "messages", v6=m == "v6", gather=m == "gather")
+        u = f.field()
+        f.init_int(u, 4)
+        f.share_n(u, 2, False)
+        chk = f.check(u, init="int", seed=4, nshares=2, compute=False)
+        assert chk.passed and chk.maxrel == 0.0, (m, chk)
+        outs.append(u)
+        f.close()
+    assert torch.equal(outs[0], outs[1])
+
+
 @pytest.mark.parametrize("args,opts", [("1 1 1 6 5 4 8 1 2 3", ["--periodic", "--init=int", "--autotune"]),
                                        ("2 1 1 5 4 3 12 1 1 2", ["--autotune"]),
                                        ("1 1 1 4 4 4 5 1 2 -5", ["--periodic", "--autotune"])])
