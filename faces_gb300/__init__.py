@@ -66,6 +66,8 @@ def lib() -> ctypes.CDLL:
                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                               ctypes.POINTER(ctypes.c_double), vp]
     L.faces_run_host.argtypes = [vp, dp, dp, c_int, c_int, vp]
+    L.faces_run_host_many.argtypes = [vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), c_int, c_int, vp]
+    L.faces_run_host_many.restype = c_int
     L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
     L.faces_autotune.argtypes = [vp, dp, c_int, c_int, vp]
@@ -293,6 +295,22 @@ class Faces:
                 raise ValueError("host buffers must be contiguous float64 arrays of the field size")
         _check(lib().faces_run_host(self._h, u_in.ctypes.data, u_out.ctypes.data, int(compute), nshares,
                                     _stream(stream)))
+
+    def run_host_many(self, u_in: list, u_out: list, nshares: int, compute: bool = True, stream=None) -> None:
+        """Independent jobs from host memory: job j uploads u_in[j], runs
+        nshares shares and downloads to u_out[j]; uploads and downloads of
+        neighbouring jobs overlap the shares (faces_run_host_many)."""
+        import numpy as np
+        if len(u_in) != len(u_out):
+            raise ValueError("one output buffer per input buffer")
+        for a in list(u_in) + list(u_out):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                    and a.size == self.total_doubles):
+                raise ValueError("host buffers must be contiguous float64 arrays of the field size")
+        nj = len(u_in)
+        ins = (ctypes.c_void_p * max(nj, 1))(*[a.ctypes.data for a in u_in])
+        outs = (ctypes.c_void_p * max(nj, 1))(*[a.ctypes.data for a in u_out])
+        _check(lib().faces_run_host_many(self._h, nj, ins, outs, int(compute), nshares, _stream(stream)))
 
     def set_tuning(self, chunk: int = 0, width: int = 0, order: int = -1) -> None:
         """Elements per x-chunk, width (row kernel: tiles per block; tile

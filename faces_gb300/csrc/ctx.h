@@ -1,6 +1,8 @@
 // ctx.h -- the context behind faces_ctx (internal to the library).
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <vector>
 
 #include "../../include/faces_gb300.h"
@@ -21,6 +23,13 @@ struct faces_ctx {
   double *d_msg = nullptr;
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
   double *d_field = nullptr;                // faces_run_host's device copy
+  // faces_run_host_many: a second device field, copy streams and the events
+  // that order uploads, shares and downloads of the two fields
+  double *d_field2 = nullptr;
+  bool pipe_ready = false;
+  cudaStream_t s_up = nullptr, s_down = nullptr;
+  cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int chunk = 0, tpb = 0, order = -1;
   int sms = 0;       // multiprocessors of the device
   faces::RowPlan plan;   // row kernel

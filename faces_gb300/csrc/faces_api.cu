@@ -191,6 +191,12 @@ int faces_destroy(faces_ctx *c)
   cudaFree(c->d_msg);
   cudaFree(c->d_scratch);
   cudaFree(c->d_field);
+  cudaFree(c->d_field2);
+  for (cudaStream_t st : {c->s_up, c->s_down})
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t e : {c->ev_up[0], c->ev_up[1], c->ev_done[0], c->ev_done[1], c->ev_free[0], c->ev_free[1],
+                        c->ev_fork, c->ev_join})
+    if (e) cudaEventDestroy(e);
   delete c;
   return FACES_OK;
 }
@@ -454,6 +460,63 @@ int faces_run_host(faces_ctx *c, const double *u_in, double *u_out, int compute,
   if (int rc = faces_share_n(c, c->d_field, compute, nshares, stream)) return rc;
   CUDA_TRY(cudaMemcpyAsync(u_out, c->d_field, bytes, cudaMemcpyDeviceToHost, s), "faces_run_host: download");
   CUDA_TRY(cudaStreamSynchronize(s), "faces_run_host: synchronize");
+  return FACES_OK;
+}
+
+int faces_run_host_many(faces_ctx *c, int njobs, const double *const *u_in, double *const *u_out, int compute,
+                        int nshares, void *stream)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (njobs < 0) return fail(FACES_EINVAL, "njobs = %d must not be negative", njobs);
+  if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
+  if (njobs == 0) return FACES_OK;
+  if (!u_in || !u_out) return fail(FACES_EINVAL, "null job array");
+  for (int j = 0; j < njobs; j++) {
+    if (!u_in[j] || !u_out[j]) return fail(FACES_EINVAL, "job %d: null host buffer", j);
+    // an upload may run while an earlier job's download is in flight
+    for (int i = 0; i < j; i++)
+      if (u_in[j] == u_out[i]) return fail(FACES_EINVAL, "job %d reads the output of job %d", j, i);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t bytes = sizeof(double) * c->total;
+  if (!c->d_field) CUDA_TRY(cudaMalloc(&c->d_field, bytes), "faces_run_host_many: device field");
+  if (njobs > 1 && !c->d_field2) CUDA_TRY(cudaMalloc(&c->d_field2, bytes), "faces_run_host_many: second field");
+  if (!c->pipe_ready) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->s_up, cudaStreamNonBlocking), "faces_run_host_many: stream");
+    CUDA_TRY(cudaStreamCreateWithFlags(&c->s_down, cudaStreamNonBlocking), "faces_run_host_many: stream");
+    cudaEvent_t *evs[8] = {&c->ev_up[0], &c->ev_up[1], &c->ev_done[0], &c->ev_done[1],
+                           &c->ev_free[0], &c->ev_free[1], &c->ev_fork, &c->ev_join};
+    for (cudaEvent_t *e : evs) CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "faces_run_host_many: event");
+    c->pipe_ready = true;
+  }
+  double *dev[2] = {c->d_field, c->d_field2};
+  // the copy streams start after the caller's earlier work on `stream`
+  CUDA_TRY(cudaEventRecord(c->ev_fork, s), "faces_run_host_many: fork");
+  CUDA_TRY(cudaStreamWaitEvent(c->s_up, c->ev_fork, 0), "faces_run_host_many: fork");
+  CUDA_TRY(cudaStreamWaitEvent(c->s_down, c->ev_fork, 0), "faces_run_host_many: fork");
+  for (int j = 0; j < njobs; j++) {
+    const int b = j & 1;
+    // job j reuses job j-2's field once that job's download is done
+    if (j >= 2) CUDA_TRY(cudaStreamWaitEvent(c->s_up, c->ev_free[b], 0), "faces_run_host_many: wait");
+    CUDA_TRY(cudaMemcpyAsync(dev[b], u_in[j], bytes, cudaMemcpyHostToDevice, c->s_up), "faces_run_host_many: upload");
+    CUDA_TRY(cudaEventRecord(c->ev_up[b], c->s_up), "faces_run_host_many: event");
+    CUDA_TRY(cudaStreamWaitEvent(s, c->ev_up[b], 0), "faces_run_host_many: wait");
+    if (int rc = faces_share_n(c, dev[b], compute, nshares, stream)) {
+      // no copy of this call stays in flight behind an error
+      cudaStreamSynchronize(c->s_up);
+      cudaStreamSynchronize(c->s_down);
+      return rc;
+    }
+    CUDA_TRY(cudaEventRecord(c->ev_done[b], s), "faces_run_host_many: event");
+    CUDA_TRY(cudaStreamWaitEvent(c->s_down, c->ev_done[b], 0), "faces_run_host_many: wait");
+    CUDA_TRY(cudaMemcpyAsync(u_out[j], dev[b], bytes, cudaMemcpyDeviceToHost, c->s_down),
+             "faces_run_host_many: download");
+    CUDA_TRY(cudaEventRecord(c->ev_free[b], c->s_down), "faces_run_host_many: event");
+  }
+  // the caller's stream joins the downloads (and with them the uploads)
+  CUDA_TRY(cudaEventRecord(c->ev_join, c->s_down), "faces_run_host_many: join");
+  CUDA_TRY(cudaStreamWaitEvent(s, c->ev_join, 0), "faces_run_host_many: join");
+  CUDA_TRY(cudaStreamSynchronize(s), "faces_run_host_many: synchronize");
   return FACES_OK;
 }
 

@@ -118,6 +118,18 @@ int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long se
  * (host; may equal u_in).  Synchronous.  Pinned host memory is fastest. */
 int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int compute, int nshares, void *stream);
 
+/* faces_run_host for njobs independent fields of this context's shape: job j
+ * uploads u_in[j], runs nshares shares and downloads to u_out[j].  Two device
+ * fields and two copy streams let job j+1's upload and job j-1's download run
+ * while job j's shares run on `stream`.  u_out[j] may equal u_in[j], and
+ * outputs may repeat across jobs (downloads run in job order); an input may
+ * not be an earlier job's output (FACES_EINVAL), and buffers must not overlap
+ * otherwise.  Synchronous; the overlap needs pinned host memory.
+ * No counterpart in the reference, whose main loop holds one field per
+ * process (gpu/main.cc:169-184). */
+int faces_run_host_many(faces_ctx *ctx, int njobs, const double *const *u_in, double *const *u_out, int compute,
+                        int nshares, void *stream);
+
 /* Work decomposition: elements per x-chunk (<= 0: default; the tile kernel
  * rounds down to a power of 2, at most 8, or 16/32 for n <= 5/3), width (<= 0: default): tiles per thread
  * block for the row kernel, resident blocks per SM for the tile kernel, and

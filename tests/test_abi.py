@@ -45,6 +45,7 @@ def test_argument_errors_without_gpu(faces_lib):
         assert L.faces_create(ctypes.byref(h), *args) == -1
         assert L.faces_last_error()
     assert L.faces_share(None, None, 1, None) == -1
+    assert L.faces_run_host_many(None, 1, None, None, 1, 1, None) == -1
     assert L.faces_destroy(None) == 0
     with pytest.raises(F.FacesError):
         F.Faces(1, 1, 1, 2, 2, 2, 1)

@@ -268,3 +268,39 @@ def test_executable_autotune(faces_lib, args, opts):
     assert r.returncode == 0, r.stderr
     nranks = int(args.split()[0]) * int(args.split()[1]) * int(args.split()[2])
     assert f"{nranks} tasks passed correctness check" in r.stdout, r.stdout
+
+
+@pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
+def test_run_host_many(oracle, faces_lib, messages):
+    """faces_run_host_many (uploads and downloads overlapping the shares of
+    neighbouring jobs) gives every job the result of faces_run_host alone,
+    and the oracle's; in place, one job and no job work; an input that is an
+    earlier job's output is refused."""
+    O, F = oracle, faces_lib
+    shape = (2, 1, 1, 5, 4, 3, 6)
+    s = O.Shape(*shape, periodic=True)
+    f = F.Faces(*shape, periodic=True, messages=messages)
+    u = f.field()
+    ins = []
+    for seed in (1, 2, 3, 4, 5):
+        f.init_int(u, seed)
+        torch.cuda.synchronize()
+        ins.append(u.cpu().numpy().copy())
+    outs = [np.empty_like(a) for a in ins]
+    f.run_host_many(ins, outs, 3)
+    for seed, a, b in zip((1, 2, 3, 4, 5), ins, outs):
+        alone = np.empty_like(a)
+        f.run_host(a, alone, 3)
+        assert np.array_equal(b, alone), seed
+    assert np.array_equal(outs[2], O.groups_share(s, O.init_int(s, 3), True, 3))
+    inplace = [a.copy() for a in ins[:3]]
+    f.run_host_many(inplace, inplace, 3)
+    for a, b in zip(inplace, outs[:3]):
+        assert np.array_equal(a, b)
+    one = [np.empty_like(ins[0])]
+    f.run_host_many(ins[:1], one, 3)
+    assert np.array_equal(one[0], outs[0])
+    f.run_host_many([], [], 3)
+    with pytest.raises(F.FacesError):
+        f.run_host_many([ins[0], outs[0]], [outs[0], outs[1]], 3)
+    f.close()
