@@ -34,9 +34,9 @@ void faces_internal_set_error(const char *msg);
 namespace faces {
 
 
-RowPlan batch_plan(const FieldDesc &f, int half)
+RowPlan batch_plan(const FieldDesc &f, int half, bool lean)
 {
-  RowPlan p = make_row_plan(f, batch_n_supported(f.n) ? bk(f.n, half) : 1, 0);
+  RowPlan p = make_row_plan(f, !batch_n_supported(f.n) ? 1 : lean ? bkl(f.n, half) : bk(f.n, half), 0);
   p.order = 2;
   p.unit_chunks = 1;
   return p;
@@ -181,7 +181,8 @@ int build_units(faces_batch *b)
 int set_half(faces_batch *b, int half)
 {
   b->half = half;
-  for (size_t i = 0; i < b->h_fields.size(); i++) b->h_fields[i].p = batch_plan(b->h_fields[i].f, half);
+  for (size_t i = 0; i < b->h_fields.size(); i++)
+    b->h_fields[i].p = batch_plan(b->h_fields[i].f, half, b->h_fields[i].lean != 0);
   if (!b->h_fields.empty())
     CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * b->h_fields.size(),
                         cudaMemcpyHostToDevice),
@@ -256,8 +257,8 @@ int faces_batch_commit(faces_batch *b)
     const faces_ctx *c = b->ctx[i];
     BatchField bf;
     bf.f = c->desc(b->u[i]);
-    bf.p = batch_plan(bf.f, 0);
     bf.lean = ptile_field(bf.f) && !(c->flags & FACES_GENERAL);
+    bf.p = batch_plan(bf.f, 0, bf.lean != 0);
     b->h_fields[i] = bf;
     b->fused[i] = batch_eligible(c) ? 1 : 0;
   }

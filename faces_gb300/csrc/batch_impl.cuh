@@ -42,9 +42,28 @@ __host__ __device__ constexpr int stage_max(int n, int h)
 }
 __host__ __device__ constexpr int spt_max(int n) { return n < kBatchMinN ? 0 : cmax(bspt(n), spt_max(n - 1)); }
 
+__host__ __device__ constexpr int stage_even(int h) { return (stage_max(kBatchMaxN, h) + 1) & ~1; }
 template <int H>
-constexpr int kStage = (stage_max(kBatchMaxN, H) + 1) & ~1;
+constexpr int kStage = stage_even(H);
 constexpr int kSptMax = spt_max(kBatchMaxN);
+
+// elements per tile of the periodic step: as many as the stage holds (the
+// stage is sized by the largest n's power-of-2 tile, so smaller and odd n
+// get longer tiles than bk: n = 7 takes 6 elements, n = 9 takes 3 at h = 0),
+// at most 32.  The periodic step's loops take any tile length.
+__host__ __device__ constexpr int bkl(int n, int h)
+{
+  return (stage_even(h) - 2 * n * n) / (n * n * smem_row_stride(n)) > 32
+             ? 32
+             : (stage_even(h) - 2 * n * n) / (n * n * smem_row_stride(n));
+}
+__host__ __device__ constexpr bool bkl_fits(int n, int h)
+{
+  return n > kBatchMaxN || (bkl(n, h) >= bk(n, h) && bkl(n, h) * n * n * smem_row_stride(n) + 2 * n * n <= stage_even(h) &&
+                            bkl_fits(n + 1, h));
+}
+static_assert(bkl_fits(kBatchMinN, 0) && bkl_fits(kBatchMinN, 1) && bkl_fits(kBatchMinN, 2),
+              "periodic-step tiles fit the stage");
 
 // shared memory: data stages, then per-stage row arrays sized for n = 10
 constexpr long batch_smem_bytes(int h)
@@ -133,8 +152,8 @@ __device__ __forceinline__ void bstage(const BatchField &bf, const TileCursor &u
                                        SlotCol (&col)[kSptMax], const Smem &m, int st)
 {
   if (MODE == 1 || (MODE == 2 && bf.lean))
-    ptile::pstage<N, bk(N, H)>(bf.f, bf.p, u, m.data + (long)st * kStage<H>, m.meta + st, m.tinfo + st,
-                               threadIdx.x);
+    ptile::pstage<N, bkl(N, H)>(bf.f, bf.p, u, m.data + (long)st * kStage<H>, m.meta + st, m.tinfo + st,
+                                threadIdx.x);
   else
     stage_tile<N, bk(N, H), bspt(N)>(bf.f, bf.p, u, ck, have_col, col, m.data + (long)st * kStage<H>,
                                   m.rfl + st * kNNMax, m.lop + st * kNNMax, m.rinfo + st * kNNMax, m.tinfo + st);
@@ -258,7 +277,7 @@ __global__ void __launch_bounds__(256, bblocks(H))
       switch (n) {
 #define FACES_BSUM(NV)                                                       \
   case NV:                                                                   \
-    if (lean) ptile::pxpass<NV, bk(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);             \
+    if (lean) ptile::pxpass<NV, bkl(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);            \
     else sum_tile<NV, bk(NV, H)>(buf, rfl, nk, hx, regular != 0);               \
     break;
         FACES_BSUM(2) FACES_BSUM(3) FACES_BSUM(4) FACES_BSUM(5) FACES_BSUM(6) FACES_BSUM(7) FACES_BSUM(8)
@@ -273,7 +292,7 @@ __global__ void __launch_bounds__(256, bblocks(H))
 #define FACES_BSTORE(NV)                                                                                  \
   case NV:                                                                                                 \
     if (lean)                                                                                              \
-      ptile::pyzpass<NV, bk(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);                                 \
+      ptile::pyzpass<NV, bkl(NV, H)>(fu, buf, m.meta + s, nk, threadIdx.x);                                \
     else                                                                                                   \
       store_tile<NV, bk(NV, H), bspt(NV)>(buf, rfl, m.lop + s * kNNMax, m.rinfo + s * kNNMax, ti.x, nk, hx); \
     break;

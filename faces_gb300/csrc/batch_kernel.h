@@ -29,8 +29,9 @@ struct BatchUnit {
 inline bool batch_n_supported(int n) { return n >= kBatchMinN && n <= kBatchMaxN; }
 
 // the tile plan of a field in the batched kernel (half = 1: half-length
-// tiles, for the periodic-step form that keeps 4 blocks per SM)
-RowPlan batch_plan(const FieldDesc &f, int half = 0);
+// tiles, for the periodic-step form that keeps 4 blocks per SM); lean: the
+// field takes the periodic step, whose tiles fill the stage
+RowPlan batch_plan(const FieldDesc &f, int half, bool lean);
 
 // resident blocks per SM (3, or 4 with half-length tiles)
 int batch_blocks_per_sm(int half = 0);

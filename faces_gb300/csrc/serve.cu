@@ -301,7 +301,7 @@ int rebuild_tables(faces_server *s, Tick &t)
   fields.reserve(order.size());
   for (long long id : order) {
     const Job &job = s->jobs[id];
-    const RowPlan p = batch_plan(job.f, half);
+    const RowPlan p = batch_plan(job.f, half, ptile_field(job.f));
     append_units(units, (int)fields.size(), p, s->unit_div);
     fields.push_back({job.f, p, ptile_field(job.f) ? 1 : 0});
   }
