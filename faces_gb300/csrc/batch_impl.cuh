@@ -18,9 +18,10 @@ using namespace tiledev;
 
 namespace {
 
-// elements per tile for each n: as many as fit a ~20 KB stage, a power of 2
-// (h = 1: half as many, so that stages are small enough for 4 resident
-// blocks per SM; h = 2: as many as fit ~28 KB, 2 resident blocks per SM)
+// elements per tile of the general step for each n, and the tiles that size
+// the stage: as many as fit ~20 KB, a power of 2 (h = 1: half as many, so
+// that stages are small enough for 4 resident blocks per SM; h = 2: as many
+// as fit ~28 KB, 2 resident blocks per SM)
 __host__ __device__ constexpr int pow2_floor(int k) { return k >= 32 ? 32 : k >= 16 ? 16 : k >= 8 ? 8 : k >= 4 ? 4 : k >= 2 ? 2 : 1; }
 __host__ __device__ constexpr int bk(int n, int h)
 {
@@ -47,10 +48,11 @@ template <int H>
 constexpr int kStage = stage_even(H);
 constexpr int kSptMax = spt_max(kBatchMaxN);
 
-// elements per tile of the periodic step: as many as the stage holds (the
-// stage is sized by the largest n's power-of-2 tile, so smaller and odd n
-// get longer tiles than bk: n = 7 takes 6 elements, n = 9 takes 3 at h = 0),
-// at most 32.  The periodic step's loops take any tile length.
+// elements per tile of the periodic step: as many as the stage holds, at
+// most 32.  The stage is sized by the n whose power-of-2 tile needs the most
+// room (n = 8 at h = 0), so the other n get longer tiles than bk (at h = 0:
+// n = 4 takes 27 elements, 5: 17, 6: 9, 7: 6, 9: 3).  The periodic step's
+// loops take any tile length.
 __host__ __device__ constexpr int bkl(int n, int h)
 {
   return (stage_even(h) - 2 * n * n) / (n * n * smem_row_stride(n)) > 32
