@@ -219,9 +219,10 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream);
 
 /* Work list settings: unit_div (units are 1/unit_div of a column's
  * x-chunks; <= 0 keeps it), resident blocks per SM (<= 0 keeps it), half
- * (tile length: 0 default; 1 half-length tiles, whose smaller stages keep 4
- * blocks per SM; 2 tiles of up to ~28 KB, 2 blocks per SM; 1 and 2 only when
- * every batched field is periodic and in direct mode; < 0 keeps it), run
+ * (stage size: 0 default, ~20 KB; 1 half-size stages, which keep 4 blocks
+ * per SM; 2 stages of up to ~28 KB, 2 blocks per SM; 1 and 2 only when every
+ * batched field is periodic and in direct mode; < 0 keeps it -- periodic-step
+ * tiles take as many elements as the stage holds), run
  * (units a block takes in a row before striding by the grid; <= 0 keeps it). */
 int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half, int run);
 
