@@ -41,20 +41,26 @@ namespace ptile {
 using namespace tiledev;
 
 template <int N>
-__device__ __forceinline__ long col_off(const FieldDesc &f, const TileCursor &u, int s, bool xlower, int jx)
+__host__ __device__ __forceinline__ long col_off(const FieldDesc &f, const TileCursor &u, int s, bool xlower, int jx)
 {
   const bool ly = (s & 1) != 0, lz = (s & 2) != 0;
   const int dy = (ly && u.jy == 0) ? -1 : 0, dz = (lz && u.jz == 0) ? -1 : 0, dx = xlower ? -1 : 0;
   const int jy = ly ? (u.jy == 0 ? f.m[1] - 1 : u.jy - 1) : u.jy;
   const int jz = lz ? (u.jz == 0 ? f.m[2] - 1 : u.jz - 1) : u.jz;
   int q = u.r;
-  if (f.nranks > 1 && (dx | dy | dz)) q = __ldg(f.nbr + u.r * 27 + dir_index(dx, dy, dz));
+  if (f.nranks > 1 && (dx | dy | dz)) {
+#ifdef __CUDA_ARCH__
+    q = __ldg(f.nbr + u.r * 27 + dir_index(dx, dy, dz));
+#else
+    q = f.nbr[u.r * 27 + dir_index(dx, dy, dz)];
+#endif
+  }
   return (long)q * f.R + (long)jz * f.sjz + (long)jy * f.sjy + (long)jx * (N * N * N);
 }
 
 // the column of slot r
 template <int N>
-__device__ __forceinline__ int col_sel(int sy, int sz)
+__host__ __device__ __forceinline__ int col_sel(int sy, int sz)
 {
   return (sy == N - 1 ? 1 : 0) | (sz == N - 1 ? 2 : 0);
 }
@@ -69,7 +75,7 @@ struct Needed {
 };
 
 template <int N>
-__device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, int &pc)
+__host__ __device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, int &pc)
 {
   constexpr int NP = Needed<N>::NP, NI = Needed<N>::NI, E = NP > 1 ? 2 : 1;
   if constexpr (NI > 0) {
@@ -94,7 +100,8 @@ __device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, int &pc)
 }
 
 // A team of T threads (a block of 256, or one warp) works on a tile; t is
-// the thread's index in its team.  Threads and needed slots: with more than
+// the thread's index in its team.  The functions also compile for the host,
+// where tests/native/ptile_emu.cu replays them thread by thread.  Threads and needed slots: with more than
 // T/2 slots per element thread t takes slots t, t+T, ... (SPT of them) for
 // every element of the tile; with fewer, KT = T/slots threads share a slot
 // and thread t takes its elements t/slots, +KT, ...  A thread decodes its
@@ -107,7 +114,7 @@ struct PSlots {
 };
 
 template <int N, int T>
-__device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
+__host__ __device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
 {
   constexpr int NE = PSlots<N, T>::NE, KT = PSlots<N, T>::KT;
   if constexpr (KT > 1) {
@@ -123,7 +130,7 @@ __device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
 
 // Stage tile u: the needed pieces of its elements, and the x-lower ends.
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPlan &p, const TileCursor &u, double *buf,
+__host__ __device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPlan &p, const TileCursor &u, double *buf,
                                        PMeta *meta, int4 *tinfo, int t)
 {
   // one copy of the description (the batched kernel reads it from global
@@ -133,7 +140,7 @@ __device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPlan &p, co
   constexpr int KT = PSlots<N, T>::KT, SPT = PSlots<N, T>::SPT;
   constexpr long N3 = (long)N * N * N;
   const int jx0 = u.c * p.chunk;
-  const int nk = min(p.chunk, f.m[0] - jx0);
+  const int nk = p.chunk < f.m[0] - jx0 ? p.chunk : f.m[0] - jx0;
   const bool first = u.c == 0;
   const int jxl = first ? f.m[0] - 1 : jx0 - 1;
   if (t < 4) {
@@ -174,7 +181,7 @@ __device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPlan &p, co
 // The order is the general step's (x, then y, then z pairs) and every stored
 // cell is one the general step stores, without the unchanged ones.
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pxpass(double *__restrict__ u, double *buf, const PMeta *meta, int nk, int t)
+__host__ __device__ __forceinline__ void pxpass(double *__restrict__ u, double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
@@ -199,7 +206,7 @@ __device__ __forceinline__ void pxpass(double *__restrict__ u, double *buf, cons
 }
 
 template <int N, int K, int T = 256>
-__device__ __forceinline__ void pyzpass(double *__restrict__ u, const double *buf, const PMeta *meta, int nk, int t)
+__host__ __device__ __forceinline__ void pyzpass(double *__restrict__ u, const double *buf, const PMeta *meta, int nk, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;

@@ -13,19 +13,35 @@ namespace faces {
 
 namespace tiledev {
 
-__device__ __forceinline__ void cp_async(double *dst, const double *src, int len)
+// The host versions serve the CPU replay of the periodic step
+// (tests/native/ptile_emu.cu): a copy is done at once, groups are no-ops.
+__host__ __device__ __forceinline__ void cp_async(double *dst, const double *src, int len)
 {
+#ifdef __CUDA_ARCH__
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   if (len == 2)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
   else
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+#else
+  for (int i = 0; i < len; i++) dst[i] = src[i];
+#endif
 }
 
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__host__ __device__ __forceinline__ void cp_commit()
+{
+#ifdef __CUDA_ARCH__
+  asm volatile("cp.async.commit_group;" ::: "memory");
+#endif
+}
 
 template <int W>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(W) : "memory"); }
+__host__ __device__ __forceinline__ void cp_wait()
+{
+#ifdef __CUDA_ARCH__
+  asm volatile("cp.async.wait_group %0;" ::"n"(W) : "memory");
+#endif
+}
 
 struct ColKey {
   int r, jy, jz;

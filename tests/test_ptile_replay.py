@@ -1,0 +1,84 @@
+"""CPU replay of the periodic tile step (tests/native/ptile_emu.cu): the
+step's own pstage / pxpass / pyzpass, run thread by thread on the host for
+every tile, with the stage at the kernel's exact size between guard cells,
+under a model where tiles read the share's starting field and the threads
+of a phase read the cells as they were before it.  The result must equal
+the oracle bit for bit, for block (256) and warp (32) teams and for the
+tile lengths both kernels use: the single-field powers of 2 and the
+batched kernel's stage-filling lengths."""
+import ctypes
+import os
+import shutil
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "native"))
+import build_emu  # noqa: E402
+
+if not (shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
+    pytest.skip("nvcc is needed to build the replay", allow_module_level=True)
+
+_emu = None
+
+
+def emu():
+    global _emu
+    if _emu is None:
+        L = ctypes.CDLL(build_emu.build_ptile())
+        L.ptile_emulate.argtypes = [ctypes.c_int] * 9 + [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                                         ctypes.c_char_p, ctypes.c_int]
+        L.ptile_emulate.restype = ctypes.c_int
+        _emu = L
+    return _emu
+
+
+def row_stride(n):
+    return n + 2 if n % 2 == 0 else n + 1
+
+
+def tile_kmax(n):
+    v = 20480 // (n * n * row_stride(n) * 8)
+    return next((k for k in (32, 16, 8, 4, 2) if v >= k), 1)
+
+
+def batch_tile(n, stage=2688):
+    """the batched kernel's periodic-step tile length at the default stage
+    (sized by n = 8's 4-element tile: 2688 doubles)"""
+    return min(32, (stage - 2 * n * n) // (n * n * row_stride(n)))
+
+
+def cases():
+    out = []
+    for n in range(2, 13):
+        ks = sorted({1, 2, tile_kmax(n)} | ({batch_tile(n)} if n <= 10 else set()))
+        for K in ks:
+            out.append((n, K, 256))
+        out.append((n, tile_kmax(n), 32))
+    return out
+
+
+@pytest.mark.parametrize("n,K,T", cases(), ids=lambda v: str(v))
+@pytest.mark.parametrize("grid", [(1, 1, 1), (2, 1, 2)], ids=["1rank", "2x1x2"])
+def test_ptile_replay_matches_oracle(oracle, n, K, T, grid):
+    O = oracle
+    mx = min(K, 32) + 3 if K > 2 else 5
+    s = O.Shape(*grid, mx, 3, 2, n, periodic=True)
+    rng = np.random.default_rng(n * 100 + K)
+    u0 = O.init_int(s, 3)
+    m = u0 != 0
+    u0[m] = rng.standard_normal(m.sum())
+    u = u0.copy()
+    err = ctypes.create_string_buffer(256)
+    rc = emu().ptile_emulate(*grid, mx, 3, 2, n, K, T, u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, err,
+                             256)
+    assert rc == 0, err.value.decode()
+    exp = O.groups_share(s, u0.copy(), True, 2)
+    assert np.array_equal(u, exp), f"{np.count_nonzero(u != exp)} points differ"
+
+
+def test_batch_tile_lengths():
+    """the lengths replayed above are the batched kernel's (n = 4: 27, 5: 17,
+    6: 9, 7: 6, 8: 4, 9: 3, 10: 2)"""
+    assert [batch_tile(n) for n in range(4, 11)] == [27, 17, 9, 6, 4, 3, 2]
