@@ -49,13 +49,20 @@ def batch_tile(n, stage=2688):
     return min(32, (stage - 2 * n * n) // (n * n * row_stride(n)))
 
 
+def tile_kwarp(n):
+    """the warp form's tile length (about 6 KB of stage)"""
+    v = 6144 // (n * n * row_stride(n) * 8)
+    return next((k for k in (32, 16, 8, 4, 2) if v >= k), 1)
+
+
 def cases():
     out = []
     for n in range(2, 13):
         ks = sorted({1, 2, tile_kmax(n)} | ({batch_tile(n)} if n <= 10 else set()))
         for K in ks:
             out.append((n, K, 256))
-        out.append((n, tile_kmax(n), 32))
+        for K in sorted({tile_kmax(n), tile_kwarp(n)}):
+            out.append((n, K, 32))
     return out
 
 
