@@ -20,9 +20,15 @@ roofline  = the periodic tile kernel against MEASURED_PEAKS.json's copy bandwidt
 cpu_baseline = the reference's v-26 pack/inner/unpack loops transcribed to
             host C with OpenMP (the oracle), timed on this host's cores
 
---impl reference times that CPU implementation alone (the reference's own
-Mugs/Faces code cannot run on this machine: see the design doc).
+--impl reference times that CPU implementation alone.
 
+c3       = 3x3x3 periodic virtual ranks of 16^3 elements, n=6: 26 messages
+            per rank packed, swapped by buffer and unpack-added (v-26), with
+            direct mode and v-6 beside it; GB/s over field and message bytes
+reference_gpu = the reference's own CUDA build (gpu/main.cc + v-26 Faces.cc,
+            one-rank MPI stand-in, built by baseline/Makefile where its
+            sources are staged) against this repository's `faces` executable
+            on the same stdin, open mode (the reference has no periodic mode)
 batched  = 512 fields of mixed shape advanced by one persistent launch per
             share, against one launch per field (steps/s of each)
 served   = a 400-job Poisson trace through the job server, batched and
@@ -371,12 +377,106 @@ def run_faces(args) -> dict | None:
     }
     if world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline()
+    if not args.no_c3:
+        out["c3"] = c3_leg(F, dev)
+    if world == 1 and not args.no_refgpu:
+        out["reference_gpu"] = reference_gpu_leg()
     if not args.no_mixed:
         del u
         f.close()
         torch.cuda.empty_cache()
         out["batched"] = batched_leg(F, dev)
         out["served"] = served_leg(F)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# C3: virtual ranks exchanging messages
+# ---------------------------------------------------------------------------
+
+C3_SHAPE, C3_STEPS = (3, 3, 3, 16, 16, 16, 6), 50
+
+
+def c3_message_doubles(shape, v6: bool) -> int:
+    """Message doubles of one share: v-26 -- every rank's 26 messages (faces
+    n^2 m_a m_b, edges n m_a, corners 1; gpu/v-26-messages/Faces.cc:16-27);
+    v-6 -- six face messages per rank (gpu/v-6-messages-basic/Faces.cc)."""
+    lx, ly, lz, mx, my, mz, n = shape
+    faces = n * n * (my * mz + mx * mz + mx * my)
+    edges = n * (mx + my + mz)
+    per_rank = 2 * faces if v6 else 2 * faces + 4 * edges + 8
+    return lx * ly * lz * per_rank
+
+
+def c3_leg(F, dev) -> dict:
+    """C3 at full size: 50 shares per mode, timed with CUDA events after
+    autotuning (outside the timing); each run checked against the closed
+    form of its 50 shares."""
+    import torch
+    stream = torch.cuda.current_stream(dev)
+    peak, peak_kind = hbm_peak()
+    modes = {}
+    for mode in ("messages", "direct", "v6"):
+        f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6")
+        u = f.field(dev)
+        f.init_int(u, SEED, stream)
+        if mode != "v6":
+            f.autotune(u, True, 3, stream)
+        f.init_int(u, SEED, stream)
+        for _ in range(3):
+            f.share(u, True, stream)
+        f.init_int(u, SEED, stream)
+        ms = _events_ms(lambda: f.share_n(u, C3_STEPS, True, stream), stream, 1) / C3_STEPS
+        chk = f.check(u, init="int", seed=SEED, nshares=C3_STEPS)
+        msg = 0 if mode == "direct" else c3_message_doubles(C3_SHAPE, mode == "v6")
+        b = 16 * (f.points + msg)
+        modes[mode] = {"ms_per_share": round(ms, 5), "gbs": round(b / (ms * 1e-3) / 1e9, 1),
+                       "field_gbs": round(16 * f.points / (ms * 1e-3) / 1e9, 1),
+                       "frac": round(b / (ms * 1e-3) / 1e9 / peak, 4), "bytes_per_share": b,
+                       "message_doubles": msg, "launches_per_share": f.launches_per_share(True),
+                       "tuning": f.tuning(), "check_passed": bool(chk.passed and chk.maxrel == 0.0)}
+        del u
+        f.close()
+    torch.cuda.empty_cache()
+    m = modes["messages"]
+    return {"workload": "3x3x3 periodic virtual ranks (27 subdomains in one HBM), 16^3 elements of n=6 each "
+                        f"({27 * 16 ** 3 * 216:,} points), integer-valued, {C3_STEPS} shares per mode",
+            "value": m["gbs"], "unit": "GB/s", "mode": "v-26 messages (pack, buffer swap, unpack-add)",
+            "roofline": {"bound": "hbm", "achieved": m["gbs"], "peak": peak, "frac": m["frac"],
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+            "bytes": "16 B per field point + 16 B per message double (pack write + unpack read)",
+            "modes": modes}
+
+
+# ---------------------------------------------------------------------------
+# the reference's own CUDA build beside this repository's executable
+# ---------------------------------------------------------------------------
+
+def reference_gpu_leg(timeout: float = 240.0) -> dict:
+    """The reference's gpu/main.cc with v-26 Faces.cc (FUSE_SEND, FUSE_INNER,
+    FUSE_RECV; MAXTHREADS 256), unmodified, built for sm_103a against a
+    one-rank MPI stand-in, on `1 1 1 48 48 48 8 1 1 100` -- the roofline
+    field in the reference's open mode -- and this repository's `faces`
+    executable on the same stdin.  Each prints the reference's `time` and
+    `tasks passed` lines; GB/s = 16 B per point per timed share."""
+    sys.path.insert(0, os.path.join(ROOT, "baseline"))
+    import run_gpu as RG
+    stdin = RG.ARGSETS["48cubed_n8"] + "\n"
+    exe = os.path.join(RG.BIN, "faces-v26-all-t256")
+    if not os.path.isfile(exe):
+        if not os.path.isfile(RG.SRC):
+            return {"unavailable": "the reference's sources are not staged in baseline/_ref/src"}
+        r = subprocess.run(["make", "-C", os.path.join(ROOT, "baseline"), "-s", exe], capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"unavailable": "reference build failed: " + (r.stdout + r.stderr)[-300:]}
+    ref = RG.run_one([exe], stdin, timeout)
+    ours = RG.run_one([RG.FACES], stdin, timeout)
+    out = {"stdin": stdin.strip(), "mode": "open (non-periodic), reference init, nk=1 nj=1 ni=100",
+           "reference": dict(ref, build="v-26-messages -DFUSE_SEND -DFUSE_INNER -DFUSE_RECV -DMAXTHREADS=256, "
+                                        "nvcc sm_103a (baseline/Makefile)"),
+           "faces_gb300": dict(ours, build="faces executable, default settings")}
+    if ref.get("ok") and ours.get("ok"):
+        out["speedup"] = round(ref["time_s"] / ours["time_s"], 2)
     return out
 
 
@@ -567,6 +667,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end host-buffer leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--no-c3", action="store_true", help="skip the C3 virtual-rank leg")
+    ap.add_argument("--no-refgpu", action="store_true", help="skip the reference's own CUDA build")
     ap.add_argument("--tune", default="", metavar="CHUNK,ORDER,WIDTH",
                     help="set the tile settings instead of autotuning (profiling runs)")
     ap.add_argument("--profile-c4", type=int, default=0, metavar="N",

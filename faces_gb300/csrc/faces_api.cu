@@ -429,7 +429,14 @@ int faces_check(faces_ctx *c, const double *u, int init, unsigned long long seed
     }
     const long n = c->n;
     const long per_rank = n * n * n * c->m[0] * c->m[1] * c->m[2];
-    if (where) {
+    const long points = per_rank * c->nranks;
+    if (where && p >= points) {
+      // a padding double: its rank and jz slab, the point coordinates -1
+      const long pad = c->sjz - c->sjy * c->m[1], q = p - points;
+      where[0] = (int)(q / (pad * c->m[2]));
+      for (int a = 1; a < 6; a++) where[a] = -1;
+      where[6] = (int)((q % (pad * c->m[2])) / pad);
+    } else if (where) {
       long t = p % per_rank;
       where[0] = (int)(p / per_rank);
       where[1] = (int)(t % n); t /= n;

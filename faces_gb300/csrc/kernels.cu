@@ -527,6 +527,19 @@ __device__ __forceinline__ double init_at(const FieldDesc &f, int init, uint64_t
   return int_value(seed, (long)q * f.R + elem_index(f, ix, iy, iz, jx, jy, jz));
 }
 
+// The padding doubles of a rank: the page padding at the end of each of its
+// mz jz slabs (sjz - n^3*mx*my doubles each).  Every init writes them as 0
+// and no share touches them, so a nonzero (or NaN) padding double is a write
+// out of place; it counts as relative error 1 (NaN: infinite).
+__device__ __forceinline__ void check_padding(const FieldDesc &f, long q, int &r, double &got)
+{
+  const long plane = f.sjy * f.m[1], pad = f.sjz - plane, per_rank = pad * f.m[2];
+  r = (int)(q / per_rank);
+  const long t = q - (long)r * per_rank;
+  const long jz = t / pad;
+  got = f.u[(long)r * f.R + jz * f.sjz + plane + (t - jz * pad)];
+}
+
 __global__ void check_kernel(FieldDesc f, int init, unsigned long long seed, int nshares, int compute,
                              unsigned long long *rank_max, unsigned long long *gmax, unsigned long long target,
                              unsigned long long *first, long only, double *vals)
@@ -534,9 +547,29 @@ __global__ void check_kernel(FieldDesc f, int init, unsigned long long seed, int
   const int n = f.n;
   const long per_elem = (long)n * n * n;
   const long per_rank = per_elem * f.m[0] * f.m[1] * f.m[2];
-  const long total = only >= 0 ? only + 1 : per_rank * f.nranks;
+  const long points = per_rank * f.nranks;
+  const long pad_total = (f.sjz - f.sjy * f.m[1]) * f.m[2] * f.nranks;
+  const long total = only >= 0 ? only + 1 : points + pad_total;
   const long p0 = only >= 0 ? only : 0;
   for (long p = p0 + blockIdx.x * (long)blockDim.x + threadIdx.x; p < total; p += (long)gridDim.x * blockDim.x) {
+    if (p >= points) {
+      // linear index points + q: padding double q (rank-major, slab, offset)
+      int r;
+      double got;
+      check_padding(f, p - points, r, got);
+      const double d = got == 0.0 ? 0.0 : got != got ? __longlong_as_double(0x7ff0000000000000LL) : 1.0;
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+      if (only >= 0) {
+        vals[0] = got;
+        vals[1] = 0.0;
+      } else if (target) {
+        if (bits == target) atomicMin(first, (unsigned long long)p);
+      } else if (bits) {
+        atomicMax(rank_max + r, bits);
+        atomicMax(gmax, bits);
+      }
+      continue;
+    }
     const int r = (int)(p / per_rank);
     long t = p % per_rank;
     int i[3], j[3];

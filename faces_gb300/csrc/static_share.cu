@@ -13,10 +13,14 @@
 // In host code the array's name is only a host-side stand-in, not a device
 // address; the device address is taken once per device with
 // cudaGetSymbolAddress, on that device's first call (so make the first call
-// on a device before any stream capture).  Every call uses the same array and
+// on a device before any stream capture).  The address is kept for the life
+// of the process: a device reset (cudaDeviceReset, or the primary context
+// released and created again) voids it, so a process that resets a device
+// must not call this entry point on that device afterwards.  Each device has
+// its own copy of the array.  Every call on a device uses that copy and
 // leaves its contents behind: each call rewrites the tables and the messages
-// before reading them.  Two calls that overlap on the GPU (different streams,
-// or the same field on two devices sharing nothing) race on the array.
+// before reading them.  Two calls that overlap on the same device (for
+// example on two streams that are not ordered with each other) race on it.
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -191,16 +195,19 @@ extern "C" int faces_share_static(double *u, int lx, int ly, int lz, int mx, int
     return fail(FACES_ECUDA, "faces_share_static: pack kernel: %s", cudaGetErrorString(e));
   if (compute && tile_kernel_supported(n)) {
     int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return fail(FACES_ECUDA, "faces_share_static: device query: %s", cudaGetErrorString(e));
+    // the default plan of faces_share for a message-mode field: tiles of
+    // tile_default_chunk(n) elements (halved while three stages exceed
+    // 110 KB), units of half a column, the resident blocks per SM that
+    // shared memory and the launch bounds allow
     int k = tile_default_chunk(n);
+    while (k > 1 && tile_smem_bytes(n, k) > 110 * 1024) k /= 2;
     RowPlan p = make_row_plan(f, k, 0);
     p.order = 2;
     p.unit_chunks = (p.nchunks + 1) / 2;
-    int fit = (int)((228 * 1024) / (tile_smem_bytes(n, p.chunk) + 1024));
-    if (fit > 8) fit = 8;
-    if (fit < 1) fit = 1;
-    e = launch_tiles(f, p, (long)sms * fit, s);
+    e = launch_tiles(f, p, (long)sms * tile_blocks_per_sm(n, k, false), s);
   } else {
     e = launch_gather(f, compute, s);
   }

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "geom.cuh"
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
@@ -36,6 +38,22 @@ cudaError_t wtiles_n12(const FieldDesc &f, const RowPlan &p, long grid, cudaStre
 
 // stages of the tile kernels' cp.async pipeline
 constexpr int kTileStages = 3;
+
+// A kernel's dynamic shared-memory limit (cudaFuncSetAttribute) is a
+// property of the kernel on one device.  `done` holds one bit per device
+// index on which it has been raised to `bytes`; devices 64 and up set it on
+// every launch.
+inline cudaError_t raise_smem_limit(const void *kernel, int bytes, std::atomic<unsigned long long> &done)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 // the warp-tile form: warps per block, and stages per warp: 3 where a stage
 // is at most 8 KB, else 2 (so that blocks of large n still fit several to an

@@ -275,13 +275,10 @@ inline cudaError_t launch_wtiles_n(const FieldDesc &f, const RowPlan &p, long gr
   constexpr int K = tile_kwarp(N);
   if (p.chunk > K) return cudaErrorInvalidValue;
   const size_t smem = wtile_smem_bytes(N);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  if (cudaError_t e = raise_smem_limit((const void *)wtile_kernel<N, K, wtile_stages(N), kWarpsPerBlock>, (int)smem,
+                                       configured))
+    return e;
   long blocks = (p.ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
   if (grid < blocks) blocks = grid;
   if (blocks < 1) return cudaSuccess;
@@ -297,35 +294,19 @@ inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
   if (grid < 1) return cudaSuccess;
   if (!general && !ptile_field(f)) {
     const size_t smem = tile_smem_bytes(N, K) + sizeof(PMeta) * kTileStages;
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(mtile_kernel<N, K, kTileStages>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (cudaError_t e = raise_smem_limit((const void *)mtile_kernel<N, K, kTileStages>, (int)smem, configured)) return e;
     mtile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
   } else if (general) {
     const size_t smem = tile_smem_bytes(N, K);
-    // the attribute is set once per process (one device per process)
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(tile_kernel<N, K, kTileStages>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (cudaError_t e = raise_smem_limit((const void *)tile_kernel<N, K, kTileStages>, (int)smem, configured)) return e;
     tile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
   } else {
     const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() +
                         (sizeof(PMeta) + sizeof(int4)) * kTileStages;
-    static bool configured = false;
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(ptile_kernel<N, K, kTileStages>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (cudaError_t e = raise_smem_limit((const void *)ptile_kernel<N, K, kTileStages>, (int)smem, configured)) return e;
     ptile_kernel<N, K, kTileStages><<<(unsigned)grid, 256, smem, s>>>(f, p);
   }
   return cudaGetLastError();

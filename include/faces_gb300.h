@@ -109,7 +109,11 @@ int faces_init_int(faces_ctx *ctx, double *u, unsigned long long seed, void *str
  * sum of its initial copies).  Outputs (each may be NULL): rank_maxrel[nranks]
  * the per-rank maximum relative error |u-v|/(|u|+|v|); *npass the ranks
  * below 1e-15; where[7] = rank, ix, iy, iz, jx, jy, jz of the largest error
- * and vals[2] = (u, expected) there.  Synchronous. */
+ * and vals[2] = (u, expected) there.  Beyond the reference's rule, the page
+ * padding of each jz slab must still hold the zeros both inits write: a
+ * nonzero padding double counts as relative error 1 (NaN anywhere: infinite),
+ * and where it is the largest error, where[] = rank, -1 x 5, jz.
+ * Synchronous. */
 int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long seed, int nshares, int compute,
                 double *rank_maxrel, double *maxrel, int *npass, int where[7], double vals[2], void *stream);
 
@@ -177,10 +181,13 @@ const char *faces_last_error(void);
  * doubles, held by every GPU that loads the library until the process
  * exits; a field whose tables and messages do not fit is rejected with
  * FACES_EINVAL.  The array's device address is taken on the first call on
- * each device, so make that first call before any stream capture.  All calls
- * share the array and each rewrites what it reads; calls that overlap on the
- * GPU race.  flags: FACES_PERIODIC or 0.  Stream-ordered like faces_share;
- * the result equals faces_share with FACES_MESSAGES bit for bit. */
+ * each device, so make that first call before any stream capture; it is kept
+ * until the process exits, so a device reset (cudaDeviceReset) voids it and
+ * the entry point must not be called on that device again.  Each device has
+ * its own array; all calls on one device share it and each rewrites what it
+ * reads, so calls that overlap on the same device (two unordered streams)
+ * race.  flags: FACES_PERIODIC or 0.  Stream-ordered like faces_share; the
+ * result equals faces_share with FACES_MESSAGES bit for bit. */
 int faces_share_static(double *u, int lx, int ly, int lz, int mx, int my, int mz, int n, unsigned flags,
                        int compute, void *stream);
 

@@ -18,7 +18,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libmugs_ref.so")
-REFERENCE_DIR = os.environ.get("FACES_REFERENCE_DIR", "/root/reference")
+# The reference's sources, for compiling its own Mugs as the oracle's checker:
+# FACES_REFERENCE_DIR, else the unmodified copy `make -C baseline stage` puts
+# in baseline/_ref/src (git-ignored); absent, the checker is not built.
+REFERENCE_DIR = os.environ.get("FACES_REFERENCE_DIR") or os.path.join(os.path.dirname(HERE), "baseline", "_ref", "src")
 
 
 class Geom(ctypes.Structure):

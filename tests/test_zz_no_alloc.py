@@ -67,3 +67,33 @@ def test_static_share_refuses_oversized_field(faces_lib):
     assert "static scratch holds" in msg and "faces_share with FACES_MESSAGES" in msg
     torch.cuda.synchronize()
     assert torch.count_nonzero(u) == 0  # nothing ran
+
+
+def test_static_share_allocates_nothing(faces_lib):
+    """After a first call of a shape (which loads the kernels it uses, and
+    with them the module's device array, under lazy module loading), further
+    calls leave the device's free memory (cudaMemGetInfo) and torch's
+    allocator counters unchanged: nothing is allocated or freed."""
+    F = faces_lib
+    fn = static_share(F)
+    shape = (3, 3, 3, 4, 4, 4, 6)
+    f = F.Faces(*shape, periodic=True, messages=True)
+    u = f.field()
+    f.init_int(u, 3)
+    stream = torch.cuda.current_stream().cuda_stream
+    assert fn(u.data_ptr(), *shape, F.PERIODIC, 1, stream) == 0, F.lib().faces_last_error().decode()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats()
+    for _ in range(3):
+        assert fn(u.data_ptr(), *shape, F.PERIODIC, 1, stream) == 0, F.lib().faces_last_error().decode()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    stats1 = torch.cuda.memory_stats()
+    assert free1 == free0, f"free device memory changed by {free1 - free0} bytes"
+    for key in ("allocation.all.allocated", "segment.all.allocated", "num_device_alloc"):
+        assert stats1.get(key, 0) == stats0.get(key, 0), key
+    # and the result is still the message-mode result of 4 shares
+    chk = f.check(u, init="int", seed=3, nshares=4)
+    assert chk.passed and chk.maxrel == 0.0, chk
+    f.close()
