@@ -644,7 +644,9 @@ __global__ void check_kernel(FieldDesc f, int init, unsigned long long seed, int
     const double got = f.u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
     const double denom = fabs(got) + fabs(expect);
     double d = (denom > 1e-15) ? fabs(got - expect) / denom : 0.0;
-    if (d != d) d = __longlong_as_double(0x7ff0000000000000LL);  // NaN counts as infinite error
+    // a NaN fails: under the reference's rule alone it would pass, because
+    // NaN > 1e-15 is false (gpu/main.cc:55-56); inf - inf counts the same
+    if (d != d || got != got) d = __longlong_as_double(0x7ff0000000000000LL);
     const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
     if (only >= 0) {
       vals[0] = got;

@@ -19,6 +19,7 @@
 #include "tile_ops.cuh"
 #include "tile_steps.cuh"
 #include "tiles_dispatch.h"
+#include "xtile_steps.cuh"
 
 namespace faces {
 
@@ -135,6 +136,54 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
     ptile::pxpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
     __syncthreads();
     ptile::pyzpass<N, K>(f.u, buf, meta + s, nk, threadIdx.x);
+    s = (s + 1) % NS;
+  }
+}
+
+// The message-mode tile step for periodic fields (xtile_steps.cuh): the
+// periodic step's pipeline, with remote rows and x ends read from the
+// received messages and only the rank's own copies stored.
+template <int N, int K, int NS, bool OPEN>
+__global__ void __launch_bounds__(256, 3) xtile_kernel(FieldDesc f, RowPlan p)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  extern __shared__ __align__(16) double sm[];
+  static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
+  static_assert(sizeof(XMeta) % 16 == 0, "tile records keep 16-byte alignment");
+  XMeta *meta = reinterpret_cast<XMeta *>(sm + NS * stage);
+  int4 *tinfo = reinterpret_cast<int4 *>(meta + NS);
+  TileWalk nw;
+  walk_begin(p, nw);
+  if (nw.done) return;
+  int inflight = 0;
+#pragma unroll
+  for (int j = 0; j < NS - 1; j++) {
+    if (!nw.done) {
+      xtile::xstage<N, K, OPEN>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j, threadIdx.x);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+  }
+  int s = 0;
+  for (; inflight > 0; inflight--) {
+    cp_wait<NS - 2>();
+    // the staged tile, its records, and the end of the previous tile's stores
+    __syncthreads();
+    const int4 ti = tinfo[s];
+    const int sn = (s + NS - 1) % NS;
+    if (!nw.done) {
+      xtile::xstage<N, K, OPEN>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn, threadIdx.x);
+      walk_next(p, nw);
+      inflight++;
+    } else {
+      cp_commit();
+    }
+    double *buf = sm + s * stage;
+    xtile::xxpass<N, K, OPEN>(buf, meta + s, ti.y, ti, threadIdx.x);
+    __syncthreads();
+    xtile::xyzpass<N, K, OPEN>(buf, meta + s, ti.y, ti, threadIdx.x);
     s = (s + 1) % NS;
   }
 }
@@ -292,7 +341,21 @@ inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
   static_assert(tile_stage_size<N, K>() * sizeof(double) % 16 == 0, "stage alignment");
   if (grid > p.ntiles) grid = p.ntiles;
   if (grid < 1) return cudaSuccess;
-  if (!general && !ptile_field(f)) {
+  if (!general && xtile_field(f)) {
+    const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() +
+                        (sizeof(XMeta) + sizeof(int4)) * kTileStages;
+    if (f.periodic) {
+      static std::atomic<unsigned long long> configured{0};
+      if (cudaError_t e = raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, false>, (int)smem, configured))
+        return e;
+      xtile_kernel<N, K, kTileStages, false><<<(unsigned)grid, 256, smem, s>>>(f, p);
+    } else {
+      static std::atomic<unsigned long long> configured{0};
+      if (cudaError_t e = raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, true>, (int)smem, configured))
+        return e;
+      xtile_kernel<N, K, kTileStages, true><<<(unsigned)grid, 256, smem, s>>>(f, p);
+    }
+  } else if (!general && !ptile_field(f)) {
     const size_t smem = tile_smem_bytes(N, K) + sizeof(PMeta) * kTileStages;
     static std::atomic<unsigned long long> configured{0};
     if (cudaError_t e = raise_smem_limit((const void *)mtile_kernel<N, K, kTileStages>, (int)smem, configured)) return e;

@@ -21,6 +21,14 @@
 //     store take their snapshot value afterwards, so a point the share
 //     should change but does not store stays wrong.
 // The result must equal the oracle bit for bit.
+//
+// The message-mode step (xtile_steps.cuh: xstage, xxpass, xyzpass) has its
+// own replay, xtile_emulate: every share first packs the 26 messages of
+// every rank on the host (region order of geom.cuh), then replays the tiles
+// under the same model.  The tile records' addresses must lie in the field
+// (the rank's own columns and ends) or in the messages (received ones);
+// own addresses are moved from the snapshot to the live field, so the passes
+// store into the live field, and the messages must come out unchanged.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +41,7 @@
 #include "rows_setup.cuh"
 #include "tables.h"
 #include "tile_ops.cuh"
+#include "xtile_steps.cuh"
 
 using namespace faces;
 
@@ -199,6 +208,202 @@ extern "C" int ptile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     fn(f, live.data() + kGuard, snap.data() + kGuard, total, p, e);
     if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
+    for (long i = 0; i < total && e.ok; i++) {
+      const double v = live[kGuard + i];
+      u[i] = std::isnan(v) ? snap[kGuard + i] : v;
+    }
+  }
+  if (!e.ok) {
+    snprintf(err, errlen, "%s", e.msg.c_str());
+    return -1;
+  }
+  return 0;
+}
+
+namespace {
+
+// the 26 messages of every rank from field u: message (r, dir) holds
+// region(dir) of rank r in region_pos order
+void host_pack(const FieldDesc &f, const double *u, double *msg, const std::vector<long> &off)
+{
+  const int n = f.n;
+  for (int r = 0; r < f.nranks; r++)
+    for (int dir = 0; dir < 27; dir++) {
+      if (dir == 13 || off[r * 27 + dir] < 0) continue;
+      const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
+      double *out = msg + off[r * 27 + dir];
+      int i[3], j[3];
+      for (j[2] = 0; j[2] < f.m[2]; j[2]++)
+        for (j[1] = 0; j[1] < f.m[1]; j[1]++)
+          for (j[0] = 0; j[0] < f.m[0]; j[0]++)
+            for (i[2] = 0; i[2] < n; i[2]++)
+              for (i[1] = 0; i[1] < n; i[1]++)
+                for (i[0] = 0; i[0] < n; i[0]++) {
+                  bool in = true;
+                  for (int a = 0; a < 3; a++) {
+                    if (d[a] < 0) in = in && i[a] == 0 && j[a] == 0;
+                    if (d[a] > 0) in = in && i[a] == n - 1 && j[a] == f.m[a] - 1;
+                  }
+                  if (!in) continue;
+                  out[region_pos(f, d, i, j)] = u[(long)r * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2])];
+                }
+    }
+}
+
+template <int N, int K, int T, bool OPEN>
+int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, long msg_total, const RowPlan &p,
+            Err &e)
+{
+  constexpr int stage = tile_stage_size<N, K>();
+  const long ncol = p.ntiles / p.nchunks;
+  FieldDesc fs = f;
+  fs.u = snap;
+  auto in = [](const double *q, const double *b, long len) { return b && q >= b && q < b + len; };
+  std::vector<double> sm(stage + 2 * kGuard, kSentinel);
+  for (long tile = 0; tile < p.ntiles && e.ok; tile++) {
+    TileCursor u;
+    u.c = (int)(tile / ncol);
+    const long col = tile - (long)u.c * ncol, t2 = col / p.ty;
+    u.jy = (int)(col - t2 * p.ty);
+    u.jz = (int)(t2 % p.tz);
+    u.r = (int)(t2 / p.tz);
+    std::fill(sm.begin(), sm.end(), kSentinel);
+    std::fill(sm.begin() + kGuard, sm.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
+    XMeta meta{};
+    int4 tinfo = make_int4(0, 0, 0, 0);
+    for (int t = 0; t < T; t++) xtile::xstage<N, K, OPEN, T>(fs, p, u, sm.data() + kGuard, &meta, &tinfo, t);
+    const int nk = tinfo.y;
+    if (nk < 1 || nk > K || tinfo.x != u.c * p.chunk) { e.set("tile info out of range", tile); break; }
+    if (tinfo.w != meta.pcol || (!OPEN && (meta.pcol != 15 || meta.plo != 15))) {
+      e.set("presence bits inconsistent", tile);
+      break;
+    }
+    // own addresses point into the snapshot: move them to the live field;
+    // received ones must lie in the messages and are never written; absent
+    // ones are null
+    for (int sidx = 0; sidx < 4 && e.ok; sidx++) {
+      double **ps[3] = {&meta.col[sidx], &meta.lo[sidx], &meta.hi[sidx]};
+      const int pres[3] = {(meta.pcol >> sidx) & 1, (meta.plo >> sidx) & 1, (meta.phi >> sidx) & 1};
+      const int own[3] = {(meta.wcol >> sidx) & 1, (meta.wlo >> sidx) & 1, 0};
+      for (int q = 0; q < 3; q++) {
+        double *a = *ps[q];
+        if (!pres[q]) {
+          if (OPEN && a) { e.set("an absent column or end has an address", tile); break; }
+          if (own[q]) { e.set("an absent column or end marked as own", tile); break; }
+          continue;
+        }
+        if (in(a, snap, total)) {
+          if (!own[q]) { e.set("a column or end in the field not marked as own", tile); break; }
+          *ps[q] = live + (a - snap);
+        } else if (!in(a, msg, msg_total) || own[q]) {
+          e.set("tile record address outside the field and messages", tile);
+          break;
+        }
+      }
+    }
+    if (!e.ok) break;
+    phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, nk, tinfo, t); }, e, tile);
+    phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, nk, tinfo, t); }, e, tile);
+    if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
+  }
+  return e.ok ? 0 : -1;
+}
+
+using XReplayFn = int (*)(FieldDesc, double *, double *, long, double *, long, const RowPlan &, Err &);
+
+template <int N, int K>
+XReplayFn xpick_t(int T, bool open)
+{
+  if (open) return T == 32 ? xreplay<N, K, 32, true> : xreplay<N, K, 256, true>;
+  return T == 32 ? xreplay<N, K, 32, false> : xreplay<N, K, 256, false>;
+}
+
+template <int N>
+XReplayFn xpick_k(int K, int T, bool open)
+{
+  switch (K) {
+    case 1: return xpick_t<N, 1>(T, open);
+    case 2: return xpick_t<N, 2>(T, open);
+    case 4: return xpick_t<N, 4>(T, open);
+    case 8: return xpick_t<N, 8>(T, open);
+    case 16: return xpick_t<N, 16>(T, open);
+    case 32: return xpick_t<N, 32>(T, open);
+    default: return nullptr;
+  }
+}
+
+XReplayFn xpick(int n, int K, int T, bool open)
+{
+  switch (n) {
+    case 2: return xpick_k<2>(K, T, open);
+    case 3: return xpick_k<3>(K, T, open);
+    case 4: return xpick_k<4>(K, T, open);
+    case 5: return xpick_k<5>(K, T, open);
+    case 6: return xpick_k<6>(K, T, open);
+    case 7: return xpick_k<7>(K, T, open);
+    case 8: return xpick_k<8>(K, T, open);
+    case 9: return xpick_k<9>(K, T, open);
+    case 10: return xpick_k<10>(K, T, open);
+    case 11: return xpick_k<11>(K, T, open);
+    case 12: return xpick_k<12>(K, T, open);
+    default: return nullptr;
+  }
+}
+
+}  // namespace
+
+// nsteps shares of the field u (the device layout) by the message-mode
+// tile step, with tiles of K elements (the chunk) and teams of T threads:
+// periodic or open, v-26 message mode or (one open rank) direct mode.
+// Returns 0, or -1 with a message in err.
+extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int K, int T, int periodic,
+                             int messages, double *u, int nsteps, char *err, int errlen)
+{
+  Err e;
+  const XReplayFn fn = xpick(n, K, T, !periodic);
+  if (!fn || (T != 32 && T != 256)) {
+    snprintf(err, errlen, "no replay for n = %d, K = %d, T = %d", n, K, T);
+    return -1;
+  }
+  FieldDesc f{};
+  f.n = n;
+  f.m[0] = mx; f.m[1] = my; f.m[2] = mz;
+  f.L[0] = lx; f.L[1] = ly; f.L[2] = lz;
+  f.periodic = periodic ? 1 : 0;
+  f.mode = messages ? kMessages : kDirect;
+  f.nranks = lx * ly * lz;
+  f.sjy = (long)n * n * n * mx;
+  f.sjz = jz_stride(n, mx, my);
+  f.R = f.sjz * mz;
+  if (!xtile_field(f)) {
+    snprintf(err, errlen, "the message-mode step does not take this field");
+    return -1;
+  }
+  const long total = f.R * f.nranks;
+  std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
+  std::vector<long> off(nbr.size(), -1);
+  const long msg_total = messages ? message_offsets(f, nbr, off) : 0;
+  f.nbr = nbr.data();
+  f.msg_off = off.data();
+  std::vector<double> msg(msg_total + 2 * kGuard, kSentinel), msg_copy;
+  f.msg = msg.data() + kGuard;
+  std::vector<double> live(total + 2 * kGuard, kSentinel), snap(total + 2 * kGuard, kSentinel);
+  f.u = live.data() + kGuard;
+  RowPlan p = make_row_plan(f, K, 0);
+  if (p.chunk != K && K <= mx) {
+    snprintf(err, errlen, "plan chunk %d for K = %d", p.chunk, K);
+    return -1;
+  }
+  for (int step = 0; step < nsteps && e.ok; step++) {
+    std::memcpy(snap.data() + kGuard, u, sizeof(double) * total);
+    std::fill(msg.begin() + kGuard, msg.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
+    host_pack(f, u, msg.data() + kGuard, off);
+    msg_copy = msg;
+    std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
+    fn(f, live.data() + kGuard, snap.data() + kGuard, total, msg.data() + kGuard, msg_total, p, e);
+    if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
+    if (e.ok && std::memcmp(msg.data(), msg_copy.data(), sizeof(double) * msg.size()) != 0)
+      e.set("the step changed a message", -1);
     for (long i = 0; i < total && e.ok; i++) {
       const double v = live[kGuard + i];
       u[i] = std::isnan(v) ? snap[kGuard + i] : v;
