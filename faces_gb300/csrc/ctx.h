@@ -17,9 +17,11 @@ struct faces_ctx {
   long sjy, sjz, R, total;
   std::vector<int> nbr;       // [rank*27+dir]
   std::vector<long> msg_off;  // [rank*27+dir], -1: none
+  std::vector<long> recv_off; // [rank*27+dir]: what the rank receives, -1: none
   long msg_total = 0;
   int *d_nbr = nullptr;
   long *d_off = nullptr;
+  long *d_roff = nullptr;
   double *d_msg = nullptr;
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
   double *d_field = nullptr;                // faces_run_host's device copy
@@ -50,6 +52,7 @@ struct faces_ctx {
     f.nranks = nranks;
     f.msg = d_msg;
     f.msg_off = d_off;
+    f.recv_off = d_roff;
     f.nbr = d_nbr;
     return f;
   }

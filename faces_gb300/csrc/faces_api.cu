@@ -97,7 +97,8 @@ void replan(faces_ctx &c)
     // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved
     // per block) and 2048 threads of 256-thread blocks
     const bool periodic_step = (c.flags & FACES_PERIODIC) && !(c.flags & (FACES_MESSAGES | FACES_GENERAL));
-    const int fit = tile_blocks_per_sm(c.n, k, periodic_step);
+    const bool general = (c.flags & FACES_GENERAL) || c.variant == 1;
+    const int fit = tile_blocks_per_sm(c.n, k, tile_form(f, general));
     const int per_sm = c.tpb > 0 ? (c.tpb < fit ? c.tpb : fit) : fit;
     c.tgrid = (long)c.sms * (per_sm < 1 ? 1 : per_sm);
     if (periodic_step && c.order >= 0 && c.order % 16 == 3) {
@@ -158,9 +159,11 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   c->msg_off.assign(nranks * 27, -1);
   if (flags & FACES_MESSAGES) c->msg_total = message_offsets(c->desc(nullptr), c->nbr, c->msg_off);
   if (flags & FACES_V6) c->msg_total = v6_message_doubles(c->desc(nullptr));
+  c->recv_off = receive_offsets(c->nbr, c->msg_off);
   cudaError_t e;
   if ((e = cudaMalloc(&c->d_nbr, sizeof(int) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_off, sizeof(long) * nranks * 27)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_roff, sizeof(long) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_scratch, sizeof(unsigned long long) * (nranks + 4))) != cudaSuccess ||
       (c->msg_total > 0 && (e = cudaMalloc(&c->d_msg, sizeof(double) * c->msg_total)) != cudaSuccess)) {
     faces_destroy(c);
@@ -168,6 +171,8 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   }
   if ((e = cudaMemcpy(c->d_nbr, c->nbr.data(), sizeof(int) * nranks * 27, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(c->d_off, c->msg_off.data(), sizeof(long) * nranks * 27, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(c->d_roff, c->recv_off.data(), sizeof(long) * nranks * 27, cudaMemcpyHostToDevice)) !=
+          cudaSuccess ||
       (c->d_msg && (e = cudaMemset(c->d_msg, 0, sizeof(double) * c->msg_total)) != cudaSuccess)) {
     faces_destroy(c);
     return cuda_fail(e, "faces_create: upload");
@@ -188,6 +193,7 @@ int faces_destroy(faces_ctx *c)
   if (!c) return FACES_OK;
   cudaFree(c->d_nbr);
   cudaFree(c->d_off);
+  cudaFree(c->d_roff);
   cudaFree(c->d_msg);
   cudaFree(c->d_scratch);
   cudaFree(c->d_field);

@@ -47,6 +47,9 @@ struct FieldDesc {
   // the offset of rank r's buffer toward dir (-1: no neighbour there)
   double *msg;
   const long *msg_off;
+  // recv_off[r*27+dir]: offset in msg of what rank r receives from
+  // direction dir -- neighbour(r,dir)'s buffer toward -dir -- or -1
+  const long *recv_off;
   // nbr[r*27+dir]: neighbour rank in direction dir, -1 outside a
   // non-periodic grid (MPI_PROC_NULL in gpu/v-26-messages/Faces.cc:92-103)
   const int *nbr;

@@ -25,7 +25,11 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
 bool tile_kernel_supported(int n);
 int tile_default_chunk(int n);
 size_t tile_smem_bytes(int n, int chunk);
-int tile_blocks_per_sm(int n, int chunk, bool periodic_step);
+// which tile kernel a field runs (launch_tiles): the general step (or the
+// mixed one), the periodic direct step, or the message-mode step
+enum TileForm : int { kGeneralForm = 0, kPeriodicForm = 1, kExchangeForm = 2 };
+TileForm tile_form(const FieldDesc &f, bool general);
+int tile_blocks_per_sm(int n, int chunk, TileForm form);
 // the warp-tile form of the periodic step (periodic direct-mode fields; plan
 // chunk at most tile_kwarp(n)); grid in blocks of 4 warps
 size_t wtile_smem_bytes(int n);

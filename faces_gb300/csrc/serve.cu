@@ -187,7 +187,7 @@ void plain_plan(faces_server *s, Job &job)
   job.tp = make_row_plan(job.f, tile_default_chunk(n), 0);
   job.tp.order = 2;
   job.tp.unit_chunks = ptile_field(job.f) ? 1 : (job.tp.nchunks + 1) / 2;
-  job.tgrid = (long)s->sms * tile_blocks_per_sm(n, job.tp.chunk, ptile_field(job.f));
+  job.tgrid = (long)s->sms * tile_blocks_per_sm(n, job.tp.chunk, tile_form(job.f, false));
 }
 
 int admit(faces_server *s, Job &job)
@@ -210,6 +210,7 @@ int admit(faces_server *s, Job &job)
   f.R = f.sjz * j.mz;
   f.msg = nullptr;
   f.msg_off = nullptr;
+  f.recv_off = nullptr;
   f.nbr = nbr;
   plain_plan(s, job);
   cudaError_t e;

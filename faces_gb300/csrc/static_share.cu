@@ -47,9 +47,10 @@ std::mutex g_setup_mu;
 double *g_scratch_ptr[kMaxDevices] = {};
 
 // Layout of the scratch for one call: nbr (int, nranks*27, rounded to whole
-// doubles), msg_off (long, nranks*27), then the messages.  A rank's buffer
-// toward direction dir sits at a fixed offset: rank * per_rank + dir_off[dir]
-// whether or not that neighbour exists, so the offsets need no prefix sum.
+// doubles), msg_off and recv_off (long, nranks*27 each), then the messages.
+// A rank's buffer toward direction dir sits at a fixed offset: rank *
+// per_rank + dir_off[dir] whether or not that neighbour exists, so the
+// offsets need no prefix sum.
 struct StaticLayout {
   long nbr_d, off_d, msg_d, total_d;
   long per_rank;
@@ -71,7 +72,7 @@ StaticLayout static_layout(const FieldDesc &f)
   s.nbr_d = (nr27 + 1) / 2;
   s.off_d = nr27;
   s.msg_d = s.per_rank * f.nranks;
-  s.total_d = ((s.nbr_d + 31) / 32 * 32) + ((s.off_d + 31) / 32 * 32) + s.msg_d;
+  s.total_d = ((s.nbr_d + 31) / 32 * 32) + 2 * ((s.off_d + 31) / 32 * 32) + s.msg_d;
   return s;
 }
 
@@ -79,9 +80,10 @@ struct DirOffsets {
   long v[27];
 };
 
-// neighbour table and message offsets of every rank, written into the scratch
-__global__ void static_tables_kernel(int *nbr, long *off, int L0, int L1, int L2, int periodic, long per_rank,
-                                     DirOffsets dir_off, int nranks)
+// neighbour table, send and receive offsets of every rank, written into the
+// scratch
+__global__ void static_tables_kernel(int *nbr, long *off, long *roff, int L0, int L1, int L2, int periodic,
+                                     long per_rank, DirOffsets dir_off, int nranks)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nranks * 27) return;
@@ -98,9 +100,11 @@ __global__ void static_tables_kernel(int *nbr, long *off, int L0, int L1, int L2
       q[a] = (q[a] + L[a]) % L[a];
     }
   }
-  nbr[i] = ok ? (q[2] * L1 + q[1]) * L0 + q[0] : -1;
+  const int peer = (q[2] * L1 + q[1]) * L0 + q[0];
+  nbr[i] = ok ? peer : -1;
   if (dir == 13) nbr[i] = r;
   off[i] = (ok && dir != 13) ? r * per_rank + dir_off.v[dir] : -1;
+  roff[i] = (ok && dir != 13) ? peer * per_rank + dir_off.v[26 - dir] : -1;
 }
 
 }  // namespace
@@ -178,17 +182,19 @@ extern "C" int faces_share_static(double *u, int lx, int ly, int lz, int mx, int
   if (int rc = scratch_on_device(&scratch)) return rc;
   int *nbr = reinterpret_cast<int *>(scratch);
   long *off = reinterpret_cast<long *>(scratch + (lay.nbr_d + 31) / 32 * 32);
-  double *msg = scratch + (lay.nbr_d + 31) / 32 * 32 + (lay.off_d + 31) / 32 * 32;
+  long *roff = off + (lay.off_d + 31) / 32 * 32;
+  double *msg = scratch + (lay.nbr_d + 31) / 32 * 32 + 2 * ((lay.off_d + 31) / 32 * 32);
   f.nbr = nbr;
   f.msg_off = off;
+  f.recv_off = roff;
   f.msg = msg;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DirOffsets dof;
   for (int d = 0; d < 27; d++) dof.v[d] = lay.dir_off[d];
   const int items = (int)nranks * 27;
-  static_tables_kernel<<<(items + 255) / 256, 256, 0, s>>>(nbr, off, lx, ly, lz, f.periodic, lay.per_rank, dof,
-                                                          (int)nranks);
+  static_tables_kernel<<<(items + 255) / 256, 256, 0, s>>>(nbr, off, roff, lx, ly, lz, f.periodic, lay.per_rank,
+                                                          dof, (int)nranks);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(FACES_ECUDA, "faces_share_static: table kernel: %s", cudaGetErrorString(e));
   if ((e = launch_pack(f, s)) != cudaSuccess)
@@ -201,13 +207,13 @@ extern "C" int faces_share_static(double *u, int lx, int ly, int lz, int mx, int
     // the default plan of faces_share for a message-mode field: tiles of
     // tile_default_chunk(n) elements (halved while three stages exceed
     // 110 KB), units of half a column, the resident blocks per SM that
-    // shared memory and the launch bounds allow
+    // shared memory and the launch bounds of the field's tile kernel allow
     int k = tile_default_chunk(n);
     while (k > 1 && tile_smem_bytes(n, k) > 110 * 1024) k /= 2;
     RowPlan p = make_row_plan(f, k, 0);
     p.order = 2;
     p.unit_chunks = (p.nchunks + 1) / 2;
-    e = launch_tiles(f, p, (long)sms * tile_blocks_per_sm(n, k, false), s);
+    e = launch_tiles(f, p, (long)sms * tile_blocks_per_sm(n, k, tile_form(f, false)), s);
   } else {
     e = launch_gather(f, compute, s);
   }

@@ -50,4 +50,16 @@ inline long message_offsets(const FieldDesc &f, const std::vector<int> &nbr, std
   return tot;
 }
 
+// offsets of what each rank receives: recv[r*27+dir] = the offset of
+// neighbour(r,dir)'s buffer toward the opposite direction, -1 without one
+inline std::vector<long> receive_offsets(const std::vector<int> &nbr, const std::vector<long> &off)
+{
+  std::vector<long> recv(nbr.size(), -1);
+  for (size_t i = 0; i < nbr.size(); i++) {
+    const int dir = (int)(i % 27), q = nbr[i];
+    if (dir != 13 && q >= 0) recv[i] = off[q * 27 + (26 - dir)];
+  }
+  return recv;
+}
+
 }  // namespace faces

@@ -9,6 +9,7 @@
 #include "tile_ops.cuh"
 #include "tile_steps.cuh"
 #include "tiles_dispatch.h"
+#include "xtile_steps.cuh"
 
 namespace faces {
 
@@ -25,16 +26,25 @@ size_t tile_smem_bytes(int n, int chunk)
          sizeof(int4) * kTileStages;
 }
 
+TileForm tile_form(const FieldDesc &f, bool general)
+{
+  if (!general && xtile_field(f)) return kExchangeForm;
+  if (!general && ptile_field(f)) return kPeriodicForm;
+  return kGeneralForm;
+}
+
 // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved per
-// block) and the launch bounds' register budget (general 3, periodic 4)
-int tile_blocks_per_sm(int n, int chunk, bool periodic_step)
+// block) and the launch bounds' register budget (general 3, periodic and
+// message-mode 4)
+int tile_blocks_per_sm(int n, int chunk, TileForm form)
 {
   const int K = tile_instance_k(chunk);
-  const size_t smem = periodic_step ? sizeof(double) * kTileStages * tile_stage_doubles(n, K) +
-                                          (sizeof(PMeta) + sizeof(int4)) * kTileStages
-                                    : tile_smem_bytes(n, chunk);
+  const size_t data = sizeof(double) * kTileStages * tile_stage_doubles(n, K);
+  const size_t smem = form == kPeriodicForm   ? data + (sizeof(PMeta) + sizeof(int4)) * kTileStages
+                      : form == kExchangeForm ? data + sizeof(XMeta) * (kTileStages + 1)
+                                              : tile_smem_bytes(n, chunk);
   int fit = (int)((228 * 1024) / (smem + 1024));
-  const int regs_fit = periodic_step ? 4 : 3;
+  const int regs_fit = form == kGeneralForm ? 3 : 4;
   return fit < 1 ? 1 : fit > regs_fit ? regs_fit : fit;
 }
 

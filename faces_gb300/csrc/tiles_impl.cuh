@@ -140,51 +140,53 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
   }
 }
 
-// The message-mode tile step for periodic fields (xtile_steps.cuh): the
-// periodic step's pipeline, with remote rows and x ends read from the
-// received messages and only the rank's own copies stored.
+// The message-mode tile step (xtile_steps.cuh): the periodic step's
+// pipeline, with remote rows and x ends read from the received messages and
+// only the rank's own copies stored.  Tile i is described (addresses, from
+// the receive table) in iteration i-3, staged in iteration i-2 and summed in
+// iteration i: NS data stages and NS+1 records, two block barriers per tile.
 template <int N, int K, int NS, bool OPEN>
-__global__ void __launch_bounds__(256, 3) xtile_kernel(FieldDesc f, RowPlan p)
+__global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
 {
   constexpr int stage = tile_stage_size<N, K>();
+  constexpr int NR = NS + 1;
   extern __shared__ __align__(16) double sm[];
   static_assert(stage % 2 == 0, "stages must keep 16-byte alignment");
   static_assert(sizeof(XMeta) % 16 == 0, "tile records keep 16-byte alignment");
-  XMeta *meta = reinterpret_cast<XMeta *>(sm + NS * stage);
-  int4 *tinfo = reinterpret_cast<int4 *>(meta + NS);
+  XMeta *rec = reinterpret_cast<XMeta *>(sm + NS * stage);
+  const int t = threadIdx.x;
   TileWalk nw;
   walk_begin(p, nw);
   if (nw.done) return;
-  int inflight = 0;
+  int ndesc = 0;  // tiles described so far
+  for (int j = 0; j < NR - 1 && !nw.done; j++) {
+    xtile::xdescribe<N, OPEN, 256>(f, p, nw.u, rec + j, t);
+    walk_next(p, nw);
+    ndesc++;
+  }
+  __syncthreads();
 #pragma unroll
   for (int j = 0; j < NS - 1; j++) {
-    if (!nw.done) {
-      xtile::xstage<N, K, OPEN>(f, p, nw.u, sm + j * stage, meta + j, tinfo + j, threadIdx.x);
-      walk_next(p, nw);
-      inflight++;
-    } else {
-      cp_commit();
-    }
+    if (j < ndesc) xtile::xcopies<N, K, OPEN>(rec + j, sm + j * stage, t);
+    else cp_commit();
   }
-  int s = 0;
-  for (; inflight > 0; inflight--) {
+  for (int i = 0; i < ndesc; i++) {
     cp_wait<NS - 2>();
-    // the staged tile, its records, and the end of the previous tile's stores
+    // tile i's stage, the records up to i+NS-1, and the end of tile i-1's
+    // stores (its stage and record are free again)
     __syncthreads();
-    const int4 ti = tinfo[s];
-    const int sn = (s + NS - 1) % NS;
+    if (i + NS - 1 < ndesc) xtile::xcopies<N, K, OPEN>(rec + (i + NS - 1) % NR, sm + ((i + NS - 1) % NS) * stage, t);
+    else cp_commit();
+    double *buf = sm + (i % NS) * stage;
+    const XMeta *r = rec + i % NR;
+    xtile::xxpass<N, K, OPEN>(buf, r, t);
     if (!nw.done) {
-      xtile::xstage<N, K, OPEN>(f, p, nw.u, sm + sn * stage, meta + sn, tinfo + sn, threadIdx.x);
+      xtile::xdescribe<N, OPEN, 256>(f, p, nw.u, rec + (i + NR - 1) % NR, t);
       walk_next(p, nw);
-      inflight++;
-    } else {
-      cp_commit();
+      ndesc++;
     }
-    double *buf = sm + s * stage;
-    xtile::xxpass<N, K, OPEN>(buf, meta + s, ti.y, ti, threadIdx.x);
     __syncthreads();
-    xtile::xyzpass<N, K, OPEN>(buf, meta + s, ti.y, ti, threadIdx.x);
-    s = (s + 1) % NS;
+    xtile::xyzpass<N, K, OPEN>(buf, r, t);
   }
 }
 
@@ -342,8 +344,7 @@ inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
   if (grid > p.ntiles) grid = p.ntiles;
   if (grid < 1) return cudaSuccess;
   if (!general && xtile_field(f)) {
-    const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() +
-                        (sizeof(XMeta) + sizeof(int4)) * kTileStages;
+    const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() + sizeof(XMeta) * (kTileStages + 1);
     if (f.periodic) {
       static std::atomic<unsigned long long> configured{0};
       if (cudaError_t e = raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, false>, (int)smem, configured))

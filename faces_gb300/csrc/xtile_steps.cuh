@@ -1,4 +1,4 @@
-// xtile_steps.cuh -- the tile step for periodic fields in v-26 message mode.
+// xtile_steps.cuh -- the tile step for v-26 message mode (and one open rank).
 //
 // In message mode every rank sums each point of its subdomain boundary from
 // its own copies and the copies its neighbours sent (the 26 messages of
@@ -50,20 +50,24 @@ FACES_HD bool xtile_field(const FieldDesc &f)
   return f.mode == kMessages || (f.nranks == 1 && !f.periodic);
 }
 
-// Per tile: for column s (bit 0 the y-lower column, bit 1 the z-lower one),
-// the address of row (0, 0), point 0 of element jx0 and the strides of an
+// The record of one tile, written one pipeline step before its copies are
+// issued (so that the table loads behind its addresses are off the copies'
+// path): for column s (bit 0 the y-lower column, bit 1 the z-lower one) the
+// address of row (0, 0), point 0 of element jx0 and the strides of an
 // element, a y row and a z row (0 along an axis the message does not span);
 // the same for the x-lower and x-upper ends (point n-1 of element jx0-1, or
-// the received end).  wcol / wlo: bit s set where the column / lower end is
-// the rank's own memory (written back); pcol / plo / phi: bit s set where
-// the column / lower end / upper end exists (all, in a periodic field).
+// the received end).  A null address is an absent column or end (open
+// fields only).  wcol / wlo: bit s set where the column / lower end is the
+// rank's own memory (written back; own columns lie in the field at its
+// constant strides).  flags: hx (the last chunk: it takes the upper seam),
+// vy, vz (virtual top tiles).
 struct XMeta {
   double *col[4];
   double *lo[4];
   double *hi[4];
   int es[4], ys[4], zs[4];
   int lys[4], lzs[4], hys[4], hzs[4];
-  int wcol, wlo, pcol, plo, phi, pad_[3];
+  int wcol, wlo, jx0, nk, flags, pad_[3];
 };
 
 namespace xtile {
@@ -93,10 +97,8 @@ struct XEnd {
 __host__ __device__ __forceinline__ double *recv(const FieldDesc &f, int r, int dx, int dy, int dz)
 {
   if (f.mode != kMessages) return nullptr;
-  const int dir = dir_index(dx, dy, dz);
-  const int q = FACES_XLDG(f.nbr + r * 27 + dir);
-  if (q < 0) return nullptr;
-  return f.msg + FACES_XLDG(f.msg_off + q * 27 + (26 - dir));
+  const long o = FACES_XLDG(f.recv_off + r * 27 + dir_index(dx, dy, dz));
+  return o < 0 ? nullptr : f.msg + o;
 }
 
 // the y or z offset of column s: -1 below the rank, +1 above (virtual top
@@ -204,81 +206,84 @@ __host__ __device__ __forceinline__ bool row_exists(int sy, int sz, bool vy, boo
          (!OPEN || ((pcol >> ptile::col_sel<N>(sy, sz)) & 1));
 }
 
-// the column presence bits of tile u (every column of a periodic field)
-template <int N, bool OPEN>
-__host__ __device__ __forceinline__ int present_columns(const FieldDesc &f, const TileCursor &u)
-{
-  if (!OPEN) return 15;
-  int p = 0;
-  for (int s = 0; s < 4; s++) {
-    int dy, ey, dz, ez;
-    col_axis(u.jy - (s & 1), f.m[1], dy, ey);
-    col_axis(u.jz - ((s >> 1) & 1), f.m[2], dz, ez);
-    if ((dy == 0 && dz == 0) || recv(f, u.r, 0, dy, dz)) p |= 1 << s;
-  }
-  return p;
-}
-
 // a + b over the copies that exist (pa, pb), the lower copy first
 __host__ __device__ __forceinline__ double psum(double a, bool pa, double b, bool pb)
 {
   return pa ? (pb ? a + b : a) : b;
 }
 
-// Stage tile u: every existing needed piece (both end pieces of the interior
-// rows, the seam rows in full), the x-lower ends and, on the last chunk, the
-// x-upper ends; threads 0..8 leave the tile's addresses in meta for the
-// passes.  tinfo: (jx0, nk, hx | vy << 1 | vz << 2, column presence bits).
-template <int N, int K, bool OPEN, int T = 256>
-__host__ __device__ __forceinline__ void xstage(const FieldDesc &fd, const RowPlan &p, const TileCursor &u,
-                                                double *buf, XMeta *meta, int4 *tinfo, int t)
+// Describe tile u into its record, nine jobs: 0..3 the columns and their
+// lower ends, 4..7 the upper ends, 8 the flags.  Job j < 8 runs on thread
+// j*T/8 (one per warp of a block, so that their table loads wait in
+// parallel), job 8 on thread 1; the other threads of the team do nothing.
+template <int N, bool OPEN, int T = 256>
+__host__ __device__ __forceinline__ void xdescribe(const FieldDesc &f, const RowPlan &p, const TileCursor &u,
+                                                   XMeta *rec, int thread)
 {
-  const FieldDesc f = fd;
-  constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
-  constexpr int KT = ptile::PSlots<N, T>::KT, SPT = ptile::PSlots<N, T>::SPT;
+  static_assert(T % 8 == 0 && T / 8 >= 2, "eight describe jobs on distinct threads, and thread 1");
+  const int t = thread == 1 ? 8 : (thread % (T / 8) == 0 ? thread / (T / 8) : -1);
+  if (t < 0) return;
   const int jx0 = u.c * p.chunk;
-  const int nk = p.chunk < f.m[0] - jx0 ? p.chunk : f.m[0] - jx0;
   const bool hx = u.c == p.nchunks - 1;
-  const bool vy = u.jy == f.m[1], vz = u.jz == f.m[2];
-  const int pcol = present_columns<N, OPEN>(f, u);
   if (t < 4) {
     const XCol c = column<N>(f, u, jx0, t);
-    meta->col[t] = c.base;
-    meta->es[t] = c.es;
-    meta->ys[t] = c.ys;
-    meta->zs[t] = c.zs;
+    rec->col[t] = c.base;
+    rec->es[t] = c.es;
+    rec->ys[t] = c.ys;
+    rec->zs[t] = c.zs;
     const XEnd e = lower_end<N>(f, u, c, t);
-    meta->lo[t] = e.base;
-    meta->lys[t] = e.ys;
-    meta->lzs[t] = e.zs;
+    rec->lo[t] = e.base;
+    rec->lys[t] = e.ys;
+    rec->lzs[t] = e.zs;
   } else if (t < 8) {
     const int s = t - 4;
     const XEnd e = hx ? recv_end<N>(f, u, s, 1) : XEnd{nullptr, 0, 0, false};
-    meta->hi[s] = e.base;
-    meta->hys[s] = e.ys;
-    meta->hzs[s] = e.zs;
-  } else if (t == 8) {
+    rec->hi[s] = e.base;
+    rec->hys[s] = e.ys;
+    rec->hzs[s] = e.zs;
+  } else {
     // own columns: (jy', jz') inside the rank; their lower ends are own
     // past the first chunk
-    int own = 0, plo = 0, phi = 0;
+    int own = 0;
     for (int s = 0; s < 4; s++) {
       const int jy = u.jy - (s & 1), jz = u.jz - ((s >> 1) & 1);
       if (jy >= 0 && jy < f.m[1] && jz >= 0 && jz < f.m[2]) own |= 1 << s;
-      if (!OPEN) continue;
-      if (u.c > 0 ? (pcol >> s) & 1 : recv_end<N>(f, u, s, -1).base != nullptr) plo |= 1 << s;
-      if (hx && recv_end<N>(f, u, s, 1).base) phi |= 1 << s;
     }
-    meta->wcol = own;
-    meta->wlo = u.c > 0 ? own : 0;
-    meta->pcol = pcol;
-    meta->plo = OPEN ? plo : 15;
-    meta->phi = OPEN ? phi : (hx ? 15 : 0);
-    *tinfo = make_int4(jx0, nk, (hx ? 1 : 0) | (vy ? 2 : 0) | (vz ? 4 : 0), pcol);
+    rec->wcol = own;
+    rec->wlo = u.c > 0 ? own : 0;
+    rec->jx0 = jx0;
+    rec->nk = p.chunk < f.m[0] - jx0 ? p.chunk : f.m[0] - jx0;
+    rec->flags = (hx ? 1 : 0) | (u.jy == f.m[1] ? 2 : 0) | (u.jz == f.m[2] ? 4 : 0);
   }
-  // a thread's slots: most tiles have one column for all of them; the
-  // column's address is recomputed only when it changes
-  int cs = -1;
-  XCol c{};
+}
+
+// presence bits of a described tile's columns and lower ends (all, in a
+// periodic field)
+template <bool OPEN>
+__host__ __device__ __forceinline__ int present_columns(const XMeta *rec)
+{
+  if (!OPEN) return 15;
+  return (rec->col[0] ? 1 : 0) | (rec->col[1] ? 2 : 0) | (rec->col[2] ? 4 : 0) | (rec->col[3] ? 8 : 0);
+}
+
+template <bool OPEN>
+__host__ __device__ __forceinline__ int present_lower_ends(const XMeta *rec)
+{
+  if (!OPEN) return 15;
+  return (rec->lo[0] ? 1 : 0) | (rec->lo[1] ? 2 : 0) | (rec->lo[2] ? 4 : 0) | (rec->lo[3] ? 8 : 0);
+}
+
+// Stage a described tile: every existing needed piece (both end pieces of
+// the interior rows, the seam rows in full), the x-lower ends and, on the
+// last chunk, the x-upper ends, by cp.async; commits one group.
+template <int N, int K, bool OPEN, int T = 256>
+__host__ __device__ __forceinline__ void xcopies(const XMeta *rec, double *buf, int t)
+{
+  constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int KT = ptile::PSlots<N, T>::KT, SPT = ptile::PSlots<N, T>::SPT;
+  const int nk = rec->nk, fl = rec->flags;
+  const bool hx = (fl & 1) != 0, vy = (fl & 2) != 0, vz = (fl & 4) != 0;
+  const int pcol = present_columns<OPEN>(rec);
 #pragma unroll
   for (int jj = 0; jj < SPT; jj++) {
     int j, kq;
@@ -287,25 +292,21 @@ __host__ __device__ __forceinline__ void xstage(const FieldDesc &fd, const RowPl
     ptile::needed_piece<N>(j, sy, sz, pc);
     if (!row_exists<N, OPEN>(sy, sz, vy, vz, pcol)) continue;
     const int s = ptile::col_sel<N>(sy, sz);
-    if (s != cs) {
-      c = column<N>(f, u, jx0, s);
-      cs = s;
-    }
-    const double *g = c.base + (long)kq * c.es + sz * c.zs + sy * c.ys + pc * PW;
+    const int es = rec->es[s];
+    const double *g = rec->col[s] + (long)kq * es + sz * rec->zs[s] + sy * rec->ys[s] + pc * PW;
     double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
-    for (int k = kq; k < nk; k += KT, g += (long)KT * c.es, sp += KT * NN * RS) cp_async(sp, g, PW);
+    for (int k = kq; k < nk; k += KT, g += (long)KT * es, sp += KT * NN * RS) cp_async(sp, g, PW);
   }
   double *locol = buf + K * NN * RS, *hicol = locol + NN;
   for (int r = t; r < NN; r += T) {
     const int sy = r % N, sz = r / N;
     if (!row_exists<N, OPEN>(sy, sz, vy, vz, pcol)) continue;
     const int s = ptile::col_sel<N>(sy, sz);
-    const XCol cc = column<N>(f, u, jx0, s);
-    const XEnd lo = lower_end<N>(f, u, cc, s);
-    if (!OPEN || lo.base) cp_async(locol + r, lo.base + sz * lo.zs + sy * lo.ys, 1);
+    const double *lo = rec->lo[s];
+    if (!OPEN || lo) cp_async(locol + r, lo + sz * rec->lzs[s] + sy * rec->lys[s], 1);
     if (hx) {
-      const XEnd hi = recv_end<N>(f, u, s, 1);
-      if (!OPEN || hi.base) cp_async(hicol + r, hi.base + sz * hi.zs + sy * hi.ys, 1);
+      const double *hi = rec->hi[s];
+      if (!OPEN || hi) cp_async(hicol + r, hi + sz * rec->hzs[s] + sy * rec->hys[s], 1);
     }
   }
   cp_commit();
@@ -317,12 +318,13 @@ __host__ __device__ __forceinline__ void xstage(const FieldDesc &fd, const RowPl
 // the rank's own column 0) is final there and stored: point 0 of element k,
 // and point n-1 of element k-1 or the lower end where it is the rank's own.
 template <int N, int K, bool OPEN, int T = 256>
-__host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, int nk, int4 ti, int t)
+__host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
-  const bool hx = (ti.z & 1) != 0, vy = (ti.z & 2) != 0, vz = (ti.z & 4) != 0;
-  const int pcol = ti.w, plo = OPEN ? meta->plo : 15, phi = OPEN ? meta->phi : 15;
+  const int nk = meta->nk, fl = meta->flags;
+  const bool hx = (fl & 1) != 0, vy = (fl & 2) != 0, vz = (fl & 4) != 0;
+  const int pcol = present_columns<OPEN>(meta);
   double *locol = buf + K * NN * RS, *hicol = locol + NN;
   const int items = (nk + (hx ? 1 : 0)) * NN;
   for (int i = t; i < items; i += T) {
@@ -330,7 +332,7 @@ __host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, 
     const int sy = r % N, sz = r / N;
     if (!row_exists<N, OPEN>(sy, sz, vy, vz, pcol)) continue;
     const int sel = ptile::col_sel<N>(sy, sz);
-    const bool pl = k > 0 || ((plo >> sel) & 1), ph = k < nk || ((phi >> sel) & 1);
+    const bool pl = !OPEN || k > 0 || meta->lo[sel], ph = !OPEN || k < nk || meta->hi[sel];
     double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (N - 1);
     double *hi = k == nk ? hicol + r : buf + (k * NN + r) * RS;
     double s;
@@ -345,7 +347,7 @@ __host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, 
       double *g = meta->col[0] + k * N3 + sz * N * N + sy * N;
       if (k < nk) g[0] = s;
       if (k > 0) g[-N3 + (N - 1)] = s;
-      else if (meta->wlo & 1) meta->lo[0][sz * meta->lzs[0] + sy * meta->lys[0]] = s;
+      else if (meta->wlo & 1) meta->lo[0][sz * N * N + sy * N] = s;
     }
   }
 }
@@ -358,15 +360,17 @@ __host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, 
 // tile stores it as its lower end); the lower end column is stored only
 // where it is the rank's.
 template <int N, int K, bool OPEN, int T = 256>
-__host__ __device__ __forceinline__ void xyzpass(const double *buf, const XMeta *meta, int nk, int4 ti, int t)
+__host__ __device__ __forceinline__ void xyzpass(const double *buf, const XMeta *meta, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
-  const bool hx = (ti.z & 1) != 0, vy = (ti.z & 2) != 0, vz = (ti.z & 4) != 0;
+  constexpr long N3 = (long)NN * N;
+  const int nk = meta->nk, fl = meta->flags;
+  const bool hx = (fl & 1) != 0, vy = (fl & 2) != 0, vz = (fl & 4) != 0;
   const double *locol = buf + K * NN * RS;
   const int last_c = (nk - 1) * N + (N - 1);
   const int wcol = meta->wcol, wlo = meta->wlo;
-  const int pcol = ti.w, plo = OPEN ? meta->plo : 15;
+  const int pcol = present_columns<OPEN>(meta), plo = present_lower_ends<OPEN>(meta);
   for (int i = t; i < G * COLS; i += T) {
     const int g = i / COLS, c = i - g * COLS;
     // the group's rows exist?
@@ -390,15 +394,14 @@ __host__ __device__ __forceinline__ void xyzpass(const double *buf, const XMeta 
     // the copy of row (sy, sz) at this column exists
     auto present = [&](int sy, int sz) {
       if (!OPEN) return true;
-      const int sel = ptile::col_sel<N>(sy, sz);
-      return (((lo ? plo : pcol) >> sel) & 1) != 0;
+      return ((((lo ? plo : pcol) >> ptile::col_sel<N>(sy, sz)) & 1)) != 0;
     };
     // the rank's own copy of row (sy, sz) at this column, or null
+    const long off = lo ? 0 : (long)k * N3 + x;
     auto gaddr = [&](int sy, int sz) -> double * {
       const int sel = ptile::col_sel<N>(sy, sz);
-      if (lo) return (wlo >> sel) & 1 ? meta->lo[sel] + sz * meta->lzs[sel] + sy * meta->lys[sel] : nullptr;
-      return (wcol >> sel) & 1 ? meta->col[sel] + (long)k * meta->es[sel] + x + sz * meta->zs[sel] + sy * meta->ys[sel]
-                               : nullptr;
+      if (!(((lo ? wlo : wcol) >> sel) & 1)) return nullptr;
+      return (lo ? meta->lo[sel] : meta->col[sel]) + off + sz * NN + sy * N;
     };
     if (g < 2 * (N - 2)) {
       int ay, az, by, bz;

@@ -22,7 +22,7 @@
 //     should change but does not store stays wrong.
 // The result must equal the oracle bit for bit.
 //
-// The message-mode step (xtile_steps.cuh: xstage, xxpass, xyzpass) has its
+// The message-mode step (xtile_steps.cuh: xdescribe, xcopies, xxpass, xyzpass) has its
 // own replay, xtile_emulate: every share first packs the 26 messages of
 // every rank on the host (region order of geom.cuh), then replays the tiles
 // under the same model.  The tile records' addresses must lie in the field
@@ -195,6 +195,7 @@ extern "C" int ptile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   std::vector<long> off(nbr.size(), -1);
   f.nbr = nbr.data();
   f.msg_off = off.data();
+  f.recv_off = off.data();
   f.msg = nullptr;
   std::vector<double> live(total + 2 * kGuard, kSentinel), snap(total + 2 * kGuard, kSentinel);
   f.u = live.data() + kGuard;
@@ -270,25 +271,25 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
     std::fill(sm.begin(), sm.end(), kSentinel);
     std::fill(sm.begin() + kGuard, sm.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     XMeta meta{};
-    int4 tinfo = make_int4(0, 0, 0, 0);
-    for (int t = 0; t < T; t++) xtile::xstage<N, K, OPEN, T>(fs, p, u, sm.data() + kGuard, &meta, &tinfo, t);
-    const int nk = tinfo.y;
-    if (nk < 1 || nk > K || tinfo.x != u.c * p.chunk) { e.set("tile info out of range", tile); break; }
-    if (tinfo.w != meta.pcol || (!OPEN && (meta.pcol != 15 || meta.plo != 15))) {
-      e.set("presence bits inconsistent", tile);
-      break;
-    }
+    for (int t = 0; t < T; t++) xtile::xdescribe<N, OPEN, T>(fs, p, u, &meta, t);
+    const int nk = meta.nk;
+    if (nk < 1 || nk > K || meta.jx0 != u.c * p.chunk) { e.set("tile record out of range", tile); break; }
+    const bool hx = (meta.flags & 1) != 0;
+    for (int t = 0; t < T; t++) xtile::xcopies<N, K, OPEN, T>(&meta, sm.data() + kGuard, t);
     // own addresses point into the snapshot: move them to the live field;
     // received ones must lie in the messages and are never written; absent
-    // ones are null
+    // ones (open fields) are null, and every one exists in a periodic field
     for (int sidx = 0; sidx < 4 && e.ok; sidx++) {
       double **ps[3] = {&meta.col[sidx], &meta.lo[sidx], &meta.hi[sidx]};
-      const int pres[3] = {(meta.pcol >> sidx) & 1, (meta.plo >> sidx) & 1, (meta.phi >> sidx) & 1};
       const int own[3] = {(meta.wcol >> sidx) & 1, (meta.wlo >> sidx) & 1, 0};
       for (int q = 0; q < 3; q++) {
         double *a = *ps[q];
-        if (!pres[q]) {
-          if (OPEN && a) { e.set("an absent column or end has an address", tile); break; }
+        if (q == 2 && !hx) {
+          if (a) { e.set("an upper end on a chunk that is not the last", tile); break; }
+          continue;
+        }
+        if (!a) {
+          if (!OPEN) { e.set("an absent column or end in a periodic field", tile); break; }
           if (own[q]) { e.set("an absent column or end marked as own", tile); break; }
           continue;
         }
@@ -302,8 +303,8 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
       }
     }
     if (!e.ok) break;
-    phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, nk, tinfo, t); }, e, tile);
-    phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, nk, tinfo, t); }, e, tile);
+    phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
+    phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
   }
   return e.ok ? 0 : -1;
@@ -383,8 +384,10 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
   std::vector<long> off(nbr.size(), -1);
   const long msg_total = messages ? message_offsets(f, nbr, off) : 0;
+  std::vector<long> roff = receive_offsets(nbr, off);
   f.nbr = nbr.data();
   f.msg_off = off.data();
+  f.recv_off = roff.data();
   std::vector<double> msg(msg_total + 2 * kGuard, kSentinel), msg_copy;
   f.msg = msg.data() + kGuard;
   std::vector<double> live(total + 2 * kGuard, kSentinel), snap(total + 2 * kGuard, kSentinel);

@@ -337,8 +337,10 @@ extern "C" int tiles_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   long mtot = messages ? message_offsets(f, nbr, off) : 0;
   if (!messages) off.assign(nbr.size(), -1);
   std::vector<double> msg(mtot > 0 ? mtot : 1, 0.0);
+  std::vector<long> roff = receive_offsets(nbr, off);
   f.nbr = nbr.data();
   f.msg_off = off.data();
+  f.recv_off = roff.data();
   f.msg = messages ? msg.data() : nullptr;
   c.u0 = u;
   c.u1 = u + f.R * f.nranks;
@@ -386,8 +388,10 @@ extern "C" int rows_emulate(int lx, int ly, int lz, int mx, int my, int mz, int 
   long mtot = messages ? message_offsets(f, nbr, off) : 0;
   if (!messages) off.assign(nbr.size(), -1);
   std::vector<double> msg(mtot > 0 ? mtot : 1, 0.0);
+  std::vector<long> roff = receive_offsets(nbr, off);
   f.nbr = nbr.data();
   f.msg_off = off.data();
+  f.recv_off = roff.data();
   f.msg = messages ? msg.data() : nullptr;
   c.u0 = u;
   c.u1 = u + f.R * f.nranks;
