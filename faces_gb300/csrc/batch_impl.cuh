@@ -51,7 +51,7 @@ constexpr int kSptMax = spt_max(kBatchMaxN);
 // elements per tile of the periodic step: as many as the stage holds, at
 // most 32.  The stage is sized by the n whose power-of-2 tile needs the most
 // room (n = 8 at h = 0), so the other n get longer tiles than bk (at h = 0:
-// n = 4 takes 27 elements, 5: 17, 6: 9, 7: 6, 9: 3).  The periodic step's
+// n = 4 takes 27 elements, 5: 17, 6: 12, 7: 5, 9: 3).  The periodic step's
 // loops take any tile length.
 __host__ __device__ constexpr int bkl(int n, int h)
 {

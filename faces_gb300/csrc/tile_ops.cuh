@@ -12,7 +12,8 @@
 // of a warp are dense -- GB300's FP64 pipe is narrow, so this matters.
 //
 // Shared memory of one stage (doubles):
-//   buf[k][r][RS]   k < K main elements, r = sy + n*sz, RS >= n (even)
+//   buf[k][r][RS]   k < K main elements, r = sy + n*sz, RS >= n (even,
+//                   2 mod 4: smem_row_stride)
 //   locol[r]        x-lower copy of the first seam (element jx0-1, point n-1)
 //   hicol[r]        x-upper copy of the last seam (element mx, point 0)
 // and per-row metadata (RowMeta).
@@ -41,7 +42,14 @@ struct RowMeta {
   unsigned flags;
 };
 
-FACES_HD constexpr int smem_row_stride(int n) { return n % 2 == 0 ? n + 2 : n + 1; }
+// Row stride of a stage in shared memory: the smallest even stride >= n that
+// is 2 mod 4 doubles (16 mod 32 bytes).  Even keeps every row 16-byte
+// aligned for the 16-byte copies; 2 mod 4 spreads the rows of a warp's x
+// pass (one row per lane, rows RS doubles apart) over 8 of the 16 bank
+// pairs, the fewest wavefronts a 64-bit access pattern at that stride
+// allows (a stride of 0 mod 8 doubles, e.g. 8 for n = 6, put every row on
+// the same banks: 16-way conflicts).
+FACES_HD constexpr int smem_row_stride(int n) { return (n + 1) / 2 % 2 == 1 ? (n + 1) / 2 * 2 : (n + 1) / 2 * 2 + 2; }
 
 // piece = the unit of one copy instruction: 2 doubles (16 bytes) for even n,
 // 1 double for odd n (rows are then only 8-byte aligned)

@@ -137,9 +137,11 @@ ReplayFn pick_k(int K, int T)
     case 2: return pick_t<N, 2>(T);
     case 3: return pick_t<N, 3>(T);
     case 4: return pick_t<N, 4>(T);
+    case 5: return pick_t<N, 5>(T);
     case 6: return pick_t<N, 6>(T);
     case 8: return pick_t<N, 8>(T);
     case 9: return pick_t<N, 9>(T);
+    case 12: return pick_t<N, 12>(T);
     case 16: return pick_t<N, 16>(T);
     case 17: return pick_t<N, 17>(T);
     case 27: return pick_t<N, 27>(T);
