@@ -23,7 +23,6 @@ struct faces_ctx {
   long *d_off = nullptr;
   long *d_roff = nullptr;
   double *d_msg = nullptr;
-  double *d_msg2 = nullptr;  // message mode: the second buffer of chained shares
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
   double *d_field = nullptr;                // faces_run_host's device copy
   // faces_run_host_many: a second device field, copy streams and the events
@@ -54,7 +53,6 @@ struct faces_ctx {
     f.msg = d_msg;
     f.msg_off = d_off;
     f.recv_off = d_roff;
-    f.msg_next = nullptr;
     f.nbr = d_nbr;
     return f;
   }

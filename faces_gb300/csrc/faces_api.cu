@@ -165,9 +165,7 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
       (e = cudaMalloc(&c->d_off, sizeof(long) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_roff, sizeof(long) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_scratch, sizeof(unsigned long long) * (nranks + 4))) != cudaSuccess ||
-      (c->msg_total > 0 && (e = cudaMalloc(&c->d_msg, sizeof(double) * c->msg_total)) != cudaSuccess) ||
-      ((flags & FACES_MESSAGES) && c->msg_total > 0 &&
-       (e = cudaMalloc(&c->d_msg2, sizeof(double) * c->msg_total)) != cudaSuccess)) {
+      (c->msg_total > 0 && (e = cudaMalloc(&c->d_msg, sizeof(double) * c->msg_total)) != cudaSuccess)) {
     faces_destroy(c);
     return cuda_fail(e, "faces_create: device allocation");
   }
@@ -197,7 +195,6 @@ int faces_destroy(faces_ctx *c)
   cudaFree(c->d_off);
   cudaFree(c->d_roff);
   cudaFree(c->d_msg);
-  cudaFree(c->d_msg2);
   cudaFree(c->d_scratch);
   cudaFree(c->d_field);
   cudaFree(c->d_field2);
@@ -302,35 +299,11 @@ int faces_share(faces_ctx *c, double *u, int compute, void *stream)
   return share_once(c, u, compute, static_cast<cudaStream_t>(stream));
 }
 
-// Message mode through the message-mode tile step (compute = 1, the default
-// kernel): shares can be chained, each leaving the next one's messages.
-static bool chained_messages(const faces_ctx *c, int compute)
-{
-  if (!(c->flags & FACES_MESSAGES) || !compute || !c->d_msg2) return false;
-  if (c->flags & (FACES_GATHER | FACES_ROWS | FACES_GENERAL)) return false;
-  if (c->variant != 0 || c->tplan.order == 3 || !tile_kernel_supported(c->n)) return false;
-  return tile_form(c->desc(nullptr), false) == kExchangeForm;
-}
-
 int faces_share_n(faces_ctx *c, double *u, int compute, int nshares, void *stream)
 {
   if (int rc = check_ctx(c)) return rc;
   if (int rc = check_field(u)) return rc;
   if (nshares < 0) return fail(FACES_EINVAL, "nshares = %d must not be negative", nshares);
-  if (nshares >= 2 && chained_messages(c, compute)) {
-    // one pack, then share i reads buffer i % 2 and, unless it is the last,
-    // writes the messages of share i+1 into the other buffer
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    FieldDesc f = c->desc(u);
-    CUDA_TRY(launch_pack(f, s), "pack kernel launch");
-    double *buf[2] = {c->d_msg, c->d_msg2};
-    for (int i = 0; i < nshares; i++) {
-      f.msg = buf[i & 1];
-      f.msg_next = i + 1 < nshares ? buf[(i + 1) & 1] : nullptr;
-      CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, false), "tile kernel launch");
-    }
-    return FACES_OK;
-  }
   for (int i = 0; i < nshares; i++)
     if (int rc = share_once(c, u, compute, static_cast<cudaStream_t>(stream))) return rc;
   return FACES_OK;

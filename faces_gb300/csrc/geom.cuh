@@ -50,11 +50,6 @@ struct FieldDesc {
   // recv_off[r*27+dir]: offset in msg of what rank r receives from
   // direction dir -- neighbour(r,dir)'s buffer toward -dir -- or -1
   const long *recv_off;
-  // message mode, several shares in one call: the buffer (laid out as msg,
-  // offsets msg_off) in which a share leaves the next share's messages --
-  // every rank's boundary values as the share finalises them -- so that the
-  // next share needs no pack; null: the share writes none
-  double *msg_next;
   // nbr[r*27+dir]: neighbour rank in direction dir, -1 outside a
   // non-periodic grid (MPI_PROC_NULL in gpu/v-26-messages/Faces.cc:92-103)
   const int *nbr;

@@ -211,7 +211,6 @@ int admit(faces_server *s, Job &job)
   f.msg = nullptr;
   f.msg_off = nullptr;
   f.recv_off = nullptr;
-  f.msg_next = nullptr;
   f.nbr = nbr;
   plain_plan(s, job);
   cudaError_t e;

@@ -188,7 +188,6 @@ extern "C" int faces_share_static(double *u, int lx, int ly, int lz, int mx, int
   f.msg_off = off;
   f.recv_off = roff;
   f.msg = msg;
-  f.msg_next = nullptr;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DirOffsets dof;

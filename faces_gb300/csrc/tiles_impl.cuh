@@ -142,11 +142,9 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
 
 // The message-mode tile step (xtile_steps.cuh): the periodic step's
 // pipeline, with remote rows and x ends read from the received messages and
-// only the rank's own copies stored (and, with f.msg_next, the next share's
-// messages written as the final values are stored).  Tile i is described
-// (addresses, from the receive table) in iteration i-3, staged in iteration
-// i-2 and summed in iteration i: NS data stages and NS+1 records, two block
-// barriers per tile.
+// only the rank's own copies stored.  Tile i is described (addresses, from
+// the receive table) in iteration i-3, staged in iteration i-2 and summed in
+// iteration i: NS data stages and NS+1 records, two block barriers per tile.
 template <int N, int K, int NS, bool OPEN>
 __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
 {
@@ -181,19 +179,14 @@ __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
     else cp_commit();
     double *buf = sm + (i % NS) * stage;
     const XMeta *r = rec + i % NR;
-    // an open field's tiles away from its boundary are complete: they take
-    // the passes' periodic form (block-uniform)
-    const bool full = xtile::complete<OPEN>(r);
-    if (full) xtile::xxpass<N, K, false>(f, buf, r, t);
-    else xtile::xxpass<N, K, OPEN>(f, buf, r, t);
+    xtile::xxpass<N, K, OPEN>(buf, r, t);
     if (!nw.done) {
       xtile::xdescribe<N, OPEN, 256>(f, p, nw.u, rec + (i + NR - 1) % NR, t);
       walk_next(p, nw);
       ndesc++;
     }
     __syncthreads();
-    if (full) xtile::xyzpass<N, K, false>(f, buf, r, t);
-    else xtile::xyzpass<N, K, OPEN>(f, buf, r, t);
+    xtile::xyzpass<N, K, OPEN>(buf, r, t);
   }
 }
 

@@ -60,14 +60,14 @@ FACES_HD bool xtile_field(const FieldDesc &f)
 // fields only).  wcol / wlo: bit s set where the column / lower end is the
 // rank's own memory (written back; own columns lie in the field at its
 // constant strides).  flags: hx (the last chunk: it takes the upper seam),
-// vy, vz (virtual top tiles).  r, jy, jz: the tile's rank and column.
+// vy, vz (virtual top tiles).
 struct XMeta {
   double *col[4];
   double *lo[4];
   double *hi[4];
   int es[4], ys[4], zs[4];
   int lys[4], lzs[4], hys[4], hzs[4];
-  int wcol, wlo, jx0, nk, flags, r, jy, jz;
+  int wcol, wlo, jx0, nk, flags, pad_[3];
 };
 
 namespace xtile {
@@ -254,9 +254,6 @@ __host__ __device__ __forceinline__ void xdescribe(const FieldDesc &f, const Row
     rec->jx0 = jx0;
     rec->nk = p.chunk < f.m[0] - jx0 ? p.chunk : f.m[0] - jx0;
     rec->flags = (hx ? 1 : 0) | (u.jy == f.m[1] ? 2 : 0) | (u.jz == f.m[2] ? 4 : 0);
-    rec->r = u.r;
-    rec->jy = u.jy;
-    rec->jz = u.jz;
   }
 }
 
@@ -274,53 +271,6 @@ __host__ __device__ __forceinline__ int present_lower_ends(const XMeta *rec)
 {
   if (!OPEN) return 15;
   return (rec->lo[0] ? 1 : 0) | (rec->lo[1] ? 2 : 0) | (rec->lo[2] ? 4 : 0) | (rec->lo[3] ? 8 : 0);
-}
-
-// every column and x end of the tile exists (a periodic field: always; an
-// open one: away from the global boundary); such tiles take the passes'
-// periodic form
-template <bool OPEN>
-__host__ __device__ __forceinline__ bool complete(const XMeta *rec)
-{
-  if (!OPEN) return true;
-  const bool hx = (rec->flags & 1) != 0;
-  return present_columns<true>(rec) == 15 && present_lower_ends<true>(rec) == 15 &&
-         (!hx || (rec->hi[0] && rec->hi[1] && rec->hi[2] && rec->hi[3]));
-}
-
-// The next share's messages (f.msg_next): the final value v of the rank's
-// own point (ix, iy, iz) of element (ex, ey, ez) goes to every region
-// (gpu/v-26-messages/Faces.cc:16-27) it lies in -- faces, edges, corner of
-// the subdomain boundary -- whose neighbour exists, at its region position
-// (free point indices fastest, then free element indices).  This is what
-// the pack would read at the start of the next share.
-template <int N>
-__host__ __device__ __forceinline__ void send(const FieldDesc &f, int r, int ex, int ey, int ez, int ix, int iy,
-                                              int iz, double v)
-{
-  const int bx = (ex == 0 && ix == 0) ? -1 : (ex == f.m[0] - 1 && ix == N - 1) ? 1 : 0;
-  const int by = (ey == 0 && iy == 0) ? -1 : (ey == f.m[1] - 1 && iy == N - 1) ? 1 : 0;
-  const int bz = (ez == 0 && iz == 0) ? -1 : (ez == f.m[2] - 1 && iz == N - 1) ? 1 : 0;
-  if (!(bx | by | bz)) return;
-#pragma unroll
-  for (int cz = 0; cz < 2; cz++)
-#pragma unroll
-    for (int cy = 0; cy < 2; cy++)
-#pragma unroll
-      for (int cx = 0; cx < 2; cx++) {
-        if ((cx && !bx) || (cy && !by) || (cz && !bz) || !(cx | cy | cz)) continue;
-        const int dx = cx ? bx : 0, dy = cy ? by : 0, dz = cz ? bz : 0;
-        const long o = FACES_XLDG(f.msg_off + r * 27 + dir_index(dx, dy, dz));
-        if (o < 0) continue;
-        long pos = 0, mul = 1;
-        if (!dx) { pos += ix; mul = N; }
-        if (!dy) { pos += iy * mul; mul *= N; }
-        if (!dz) { pos += iz * mul; mul *= N; }
-        if (!dx) { pos += ex * mul; mul *= f.m[0]; }
-        if (!dy) { pos += ey * mul; mul *= f.m[1]; }
-        if (!dz) pos += ez * mul;
-        f.msg_next[o + pos] = v;
-      }
 }
 
 // Stage a described tile: every existing needed piece (both end pieces of
@@ -368,7 +318,7 @@ __host__ __device__ __forceinline__ void xcopies(const XMeta *rec, double *buf, 
 // the rank's own column 0) is final there and stored: point 0 of element k,
 // and point n-1 of element k-1 or the lower end where it is the rank's own.
 template <int N, int K, bool OPEN, int T = 256>
-__host__ __device__ __forceinline__ void xxpass(const FieldDesc &f, double *buf, const XMeta *meta, int t)
+__host__ __device__ __forceinline__ void xxpass(double *buf, const XMeta *meta, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
@@ -398,12 +348,6 @@ __host__ __device__ __forceinline__ void xxpass(const FieldDesc &f, double *buf,
       if (k < nk) g[0] = s;
       if (k > 0) g[-N3 + (N - 1)] = s;
       else if (meta->wlo & 1) meta->lo[0][sz * N * N + sy * N] = s;
-      // an interior row reaches the subdomain boundary only at its x ends
-      if (f.msg_next) {
-        const int ex = meta->jx0 + k;
-        if (k < nk) send<N>(f, meta->r, ex, meta->jy, meta->jz, 0, sy, sz, s);
-        if (k > 0 || (meta->wlo & 1)) send<N>(f, meta->r, ex - 1, meta->jy, meta->jz, N - 1, sy, sz, s);
-      }
     }
   }
 }
@@ -416,7 +360,7 @@ __host__ __device__ __forceinline__ void xxpass(const FieldDesc &f, double *buf,
 // tile stores it as its lower end); the lower end column is stored only
 // where it is the rank's.
 template <int N, int K, bool OPEN, int T = 256>
-__host__ __device__ __forceinline__ void xyzpass(const FieldDesc &f, const double *buf, const XMeta *meta, int t)
+__host__ __device__ __forceinline__ void xyzpass(const double *buf, const XMeta *meta, int t)
 {
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
@@ -452,16 +396,12 @@ __host__ __device__ __forceinline__ void xyzpass(const FieldDesc &f, const doubl
       if (!OPEN) return true;
       return ((((lo ? plo : pcol) >> ptile::col_sel<N>(sy, sz)) & 1)) != 0;
     };
-    // store the final value of row (sy, sz) at this column where that copy
-    // is the rank's own, and pass it on to the next share's messages
+    // the rank's own copy of row (sy, sz) at this column, or null
     const long off = lo ? 0 : (long)k * N3 + x;
-    auto put = [&](int sy, int sz, double v) {
+    auto gaddr = [&](int sy, int sz) -> double * {
       const int sel = ptile::col_sel<N>(sy, sz);
-      if (!(((lo ? wlo : wcol) >> sel) & 1)) return;
-      (lo ? meta->lo[sel] : meta->col[sel])[off + sz * NN + sy * N] = v;
-      if (f.msg_next)
-        send<N>(f, meta->r, lo ? meta->jx0 - 1 : meta->jx0 + k, meta->jy - (sel & 1), meta->jz - ((sel >> 1) & 1),
-                lo ? N - 1 : x, sy, sz, v);
+      if (!(((lo ? wlo : wcol) >> sel) & 1)) return nullptr;
+      return (lo ? meta->lo[sel] : meta->col[sel]) + off + sz * NN + sy * N;
     };
     if (g < 2 * (N - 2)) {
       int ay, az, by, bz;
@@ -472,8 +412,8 @@ __host__ __device__ __forceinline__ void xyzpass(const FieldDesc &f, const doubl
       const double s = OPEN ? psum(pa ? sb[(az * N + ay) * srs] : 0.0, pa, pb ? sb[(bz * N + by) * srs] : 0.0, pb)
                             : sb[(az * N + ay) * srs] + sb[(bz * N + by) * srs];
       if (store) {
-        put(ay, az, s);
-        put(by, bz, s);
+        if (double *p = gaddr(ay, az)) *p = s;
+        if (double *p = gaddr(by, bz)) *p = s;
       }
     } else {
       double s;
@@ -491,10 +431,10 @@ __host__ __device__ __forceinline__ void xyzpass(const FieldDesc &f, const doubl
         s = y1 + y0;
       }
       if (store) {
-        put(0, 0, s);
-        put(N - 1, 0, s);
-        put(0, N - 1, s);
-        put(N - 1, N - 1, s);
+        if (double *p = gaddr(0, 0)) *p = s;
+        if (double *p = gaddr(N - 1, 0)) *p = s;
+        if (double *p = gaddr(0, N - 1)) *p = s;
+        if (double *p = gaddr(N - 1, N - 1)) *p = s;
       }
     }
   }

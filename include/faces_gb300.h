@@ -90,12 +90,7 @@ int faces_field_free(double *u);
  * synchronize the stream for that). */
 int faces_share(faces_ctx *ctx, double *u, int compute, void *stream);
 
-/* nshares consecutive shares (the `ni` loop of gpu/main.cc:180).  In
- * FACES_MESSAGES mode with the tile step, the 26 messages of every rank are
- * packed once per call: each share writes the next share's messages (a
- * second buffer) as it stores the final boundary values, so nshares shares
- * take nshares + 1 launches; the results are those of nshares faces_share
- * calls, bit for bit. */
+/* nshares consecutive shares (the `ni` loop of gpu/main.cc:180). */
 int faces_share_n(faces_ctx *ctx, double *u, int compute, int nshares, void *stream);
 
 /* gpu/main.cc:10-19: u(ix,iy,iz,jx,jy,jz) = jz*1e4 + jy*100 + jx + iz*0.01 +
@@ -166,8 +161,7 @@ int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *str
  * tiles).  Any pointer may be NULL. */
 int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order);
 
-/* Kernel launches one faces_share call enqueues with the current settings
- * (faces_share_n in message mode: one fewer per share after the first). */
+/* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);
 
 /* Message of the last failed call on this thread ("" if none). */

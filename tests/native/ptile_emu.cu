@@ -305,14 +305,8 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
       }
     }
     if (!e.ok) break;
-    // the kernel's choice: complete tiles take the passes' periodic form
-    if (xtile::complete<OPEN>(&meta)) {
-      phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, false, T>(f, buf, &meta, t); }, e, tile);
-      phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, false, T>(f, buf, &meta, t); }, e, tile);
-    } else {
-      phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(f, buf, &meta, t); }, e, tile);
-      phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(f, buf, &meta, t); }, e, tile);
-    }
+    phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
+    phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
   }
   return e.ok ? 0 : -1;
@@ -364,12 +358,9 @@ XReplayFn xpick(int n, int K, int T, bool open)
 // nsteps shares of the field u (the device layout) by the message-mode
 // tile step, with tiles of K elements (the chunk) and teams of T threads:
 // periodic or open, v-26 message mode or (one open rank) direct mode.
-// chain (message mode): the messages are packed before the first share
-// only; every share writes the next one's into a second buffer (which
-// starts as NaN), and that buffer must equal a pack of the share's result.
 // Returns 0, or -1 with a message in err.
 extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int K, int T, int periodic,
-                             int messages, int chain, double *u, int nsteps, char *err, int errlen)
+                             int messages, double *u, int nsteps, char *err, int errlen)
 {
   Err e;
   const XReplayFn fn = xpick(n, K, T, !periodic);
@@ -400,7 +391,6 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   f.msg_off = off.data();
   f.recv_off = roff.data();
   std::vector<double> msg(msg_total + 2 * kGuard, kSentinel), msg_copy;
-  std::vector<double> next(msg_total + 2 * kGuard, kSentinel), expect(msg_total + 2 * kGuard, kSentinel);
   f.msg = msg.data() + kGuard;
   std::vector<double> live(total + 2 * kGuard, kSentinel), snap(total + 2 * kGuard, kSentinel);
   f.u = live.data() + kGuard;
@@ -409,21 +399,11 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     snprintf(err, errlen, "plan chunk %d for K = %d", p.chunk, K);
     return -1;
   }
-  const double nan = std::numeric_limits<double>::quiet_NaN();
-  chain = chain && messages;
   for (int step = 0; step < nsteps && e.ok; step++) {
     std::memcpy(snap.data() + kGuard, u, sizeof(double) * total);
-    if (!chain || step == 0) {
-      std::fill(msg.begin() + kGuard, msg.end() - kGuard, nan);
-      host_pack(f, u, msg.data() + kGuard, off);
-    }
+    std::fill(msg.begin() + kGuard, msg.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
+    host_pack(f, u, msg.data() + kGuard, off);
     msg_copy = msg;
-    f.msg = msg.data() + kGuard;
-    f.msg_next = nullptr;
-    if (chain) {
-      std::fill(next.begin() + kGuard, next.end() - kGuard, nan);
-      f.msg_next = next.data() + kGuard;
-    }
     std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     fn(f, live.data() + kGuard, snap.data() + kGuard, total, msg.data() + kGuard, msg_total, p, e);
     if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
@@ -432,14 +412,6 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     for (long i = 0; i < total && e.ok; i++) {
       const double v = live[kGuard + i];
       u[i] = std::isnan(v) ? snap[kGuard + i] : v;
-    }
-    if (chain && e.ok) {
-      // what this share left must be the pack of its result, entry for entry
-      std::fill(expect.begin() + kGuard, expect.end() - kGuard, nan);
-      host_pack(f, u, expect.data() + kGuard, off);
-      if (std::memcmp(next.data(), expect.data(), sizeof(double) * next.size()) != 0)
-        e.set("the next share's messages differ from a pack of the result", -1);
-      std::swap(msg, next);
     }
   }
   if (!e.ok) {

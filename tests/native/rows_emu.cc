@@ -342,7 +342,6 @@ extern "C" int tiles_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   f.msg_off = off.data();
   f.recv_off = roff.data();
   f.msg = messages ? msg.data() : nullptr;
-  f.msg_next = nullptr;
   c.u0 = u;
   c.u1 = u + f.R * f.nranks;
   c.m0 = messages ? msg.data() : nullptr;
@@ -394,7 +393,6 @@ extern "C" int rows_emulate(int lx, int ly, int lz, int mx, int my, int mz, int 
   f.msg_off = off.data();
   f.recv_off = roff.data();
   f.msg = messages ? msg.data() : nullptr;
-  f.msg_next = nullptr;
   c.u0 = u;
   c.u1 = u + f.R * f.nranks;
   c.m0 = messages ? msg.data() : nullptr;

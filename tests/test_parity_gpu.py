@@ -304,25 +304,3 @@ def test_run_host_many(oracle, faces_lib, messages):
     with pytest.raises(F.FacesError):
         f.run_host_many([ins[0], outs[0]], [outs[0], outs[1]], 3)
     f.close()
-
-
-@pytest.mark.parametrize("shape,periodic", [((3, 3, 3, 3, 2, 4, 6), True), ((2, 2, 1, 3, 3, 2, 5), False),
-                                            ((1, 2, 2, 5, 2, 3, 8), True)], ids=["3x3x3-p", "2x2x1-open", "1x2x2-p"])
-def test_chained_message_shares(oracle, faces_lib, shape, periodic):
-    """faces_share_n in message mode packs once and lets each share leave
-    the next one's messages: its result equals nshares faces_share calls
-    (each packing afresh) and the oracle, bit for bit."""
-    O, F = oracle, faces_lib
-    f = F.Faces(*shape, periodic=periodic, messages=True)
-    a, b = f.field(), f.field()
-    f.init_int(a, 9)
-    f.init_int(b, 9)
-    f.share_n(a, 5)
-    for _ in range(5):
-        f.share(b)
-    torch.cuda.synchronize()
-    assert torch.equal(a, b), f"{int((a != b).sum())} points differ"
-    s = O.Shape(*shape, periodic=periodic)
-    exp = O.groups_share(s, O.init_int(s, 9), True, 5)
-    assert np.array_equal(a.cpu().numpy(), exp)
-    f.close()

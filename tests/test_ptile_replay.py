@@ -100,7 +100,7 @@ def xemu():
     global _xemu
     if _xemu is None:
         L = ctypes.CDLL(build_emu.build_ptile())
-        L.xtile_emulate.argtypes = [ctypes.c_int] * 12 + [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+        L.xtile_emulate.argtypes = [ctypes.c_int] * 11 + [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                                           ctypes.c_char_p, ctypes.c_int]
         L.xtile_emulate.restype = ctypes.c_int
         _xemu = L
@@ -117,27 +117,22 @@ def xcases():
 
 
 XGRIDS = [
-    # (grid, periodic, messages, chained shares)
-    ((1, 1, 1), True, True, False),
-    ((2, 1, 2), True, True, False),
-    ((2, 1, 2), True, True, True),
-    ((2, 2, 1), False, True, False),
-    ((2, 2, 1), False, True, True),
-    ((1, 1, 1), False, True, False),
-    ((1, 1, 1), False, False, False),
+    # (grid, periodic, messages)
+    ((1, 1, 1), True, True),
+    ((2, 1, 2), True, True),
+    ((2, 2, 1), False, True),
+    ((1, 1, 1), False, True),
+    ((1, 1, 1), False, False),
 ]
 
 
 @pytest.mark.parametrize("n,K,T", xcases(), ids=lambda v: str(v))
-@pytest.mark.parametrize("grid,periodic,messages,chain", XGRIDS,
-                         ids=["1rank-p-msg", "2x1x2-p-msg", "2x1x2-p-chain", "2x2x1-open-msg", "2x2x1-open-chain",
-                              "1rank-open-msg", "1rank-open-direct"])
-def test_xtile_replay_matches_oracle(oracle, n, K, T, grid, periodic, messages, chain):
+@pytest.mark.parametrize("grid,periodic,messages", XGRIDS,
+                         ids=["1rank-p-msg", "2x1x2-p-msg", "2x2x1-open-msg", "1rank-open-msg", "1rank-open-direct"])
+def test_xtile_replay_matches_oracle(oracle, n, K, T, grid, periodic, messages):
     """The message-mode step (and the open one-rank direct step), replayed
     thread by thread, equals the oracle on random normal inputs, 2 shares;
-    the chunk leaves a partial last tile where it can.  Chained: one pack
-    before the first share, and each share's messages for the next equal a
-    pack of its result."""
+    the chunk leaves a partial last tile where it can."""
     O = oracle
     mx = K + 2 if K > 1 else 3
     s = O.Shape(*grid, mx, 3, 2, n, periodic=periodic)
@@ -147,8 +142,8 @@ def test_xtile_replay_matches_oracle(oracle, n, K, T, grid, periodic, messages, 
     u0[m] = rng.standard_normal(m.sum())
     u = u0.copy()
     err = ctypes.create_string_buffer(256)
-    rc = xemu().xtile_emulate(*grid, mx, 3, 2, n, K, T, int(periodic), int(messages), int(chain),
-                              u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 3 if chain else 2, err, 256)
+    rc = xemu().xtile_emulate(*grid, mx, 3, 2, n, K, T, int(periodic), int(messages),
+                              u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, err, 256)
     assert rc == 0, err.value.decode()
-    exp = O.groups_share(s, u0.copy(), True, 3 if chain else 2)
+    exp = O.groups_share(s, u0.copy(), True, 2)
     assert np.array_equal(u, exp), f"{np.count_nonzero(u != exp)} points differ"
