@@ -179,14 +179,19 @@ __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
     else cp_commit();
     double *buf = sm + (i % NS) * stage;
     const XMeta *r = rec + i % NR;
-    xtile::xxpass<N, K, OPEN>(buf, r, t);
+    // an open field's tiles away from its boundary are complete: they take
+    // the passes' periodic form (block-uniform)
+    const bool full = xtile::complete<OPEN>(r);
+    if (full) xtile::xxpass<N, K, false>(buf, r, t);
+    else xtile::xxpass<N, K, OPEN>(buf, r, t);
     if (!nw.done) {
       xtile::xdescribe<N, OPEN, 256>(f, p, nw.u, rec + (i + NR - 1) % NR, t);
       walk_next(p, nw);
       ndesc++;
     }
     __syncthreads();
-    xtile::xyzpass<N, K, OPEN>(buf, r, t);
+    if (full) xtile::xyzpass<N, K, false>(buf, r, t);
+    else xtile::xyzpass<N, K, OPEN>(buf, r, t);
   }
 }
 

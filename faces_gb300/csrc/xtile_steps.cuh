@@ -273,6 +273,18 @@ __host__ __device__ __forceinline__ int present_lower_ends(const XMeta *rec)
   return (rec->lo[0] ? 1 : 0) | (rec->lo[1] ? 2 : 0) | (rec->lo[2] ? 4 : 0) | (rec->lo[3] ? 8 : 0);
 }
 
+// every column and x end of the tile exists (a periodic field: always; an
+// open one: away from the global boundary); such tiles take the passes'
+// periodic form
+template <bool OPEN>
+__host__ __device__ __forceinline__ bool complete(const XMeta *rec)
+{
+  if (!OPEN) return true;
+  const bool hx = (rec->flags & 1) != 0;
+  return present_columns<true>(rec) == 15 && present_lower_ends<true>(rec) == 15 &&
+         (!hx || (rec->hi[0] && rec->hi[1] && rec->hi[2] && rec->hi[3]));
+}
+
 // Stage a described tile: every existing needed piece (both end pieces of
 // the interior rows, the seam rows in full), the x-lower ends and, on the
 // last chunk, the x-upper ends, by cp.async; commits one group.

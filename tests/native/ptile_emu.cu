@@ -305,8 +305,14 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
       }
     }
     if (!e.ok) break;
-    phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
-    phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
+    // the kernel's choice: complete tiles take the passes' periodic form
+    if (xtile::complete<OPEN>(&meta)) {
+      phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, false, T>(buf, &meta, t); }, e, tile);
+      phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, false, T>(buf, &meta, t); }, e, tile);
+    } else {
+      phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
+      phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
+    }
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
   }
   return e.ok ? 0 : -1;
