@@ -63,6 +63,15 @@ struct Err {
   }
 };
 
+// the live field starts a share as NaN: a point a tile changes that was
+// not NaN before the tile has been written twice in the share
+void written_once(const std::vector<double> &before, const double *live, long total, Err &e, long tile)
+{
+  for (long i = 0; i < total && e.ok; i++)
+    if (std::memcmp(&before[i], live + i, sizeof(double)) != 0 && !std::isnan(before[i]))
+      e.set("a field point written twice in one share", tile);
+}
+
 bool guards_intact(const std::vector<double> &v, long inner)
 {
   for (long i = 0; i < kGuard; i++)
@@ -113,8 +122,10 @@ int replay(FieldDesc f, double *live, double *snap, long total, const RowPlan &p
     if (meta.u != snap) { e.set("tile meta names another field", tile); break; }
     const int nk = tinfo.y;
     if (nk < 1 || nk > K || tinfo.x != u.c * p.chunk) { e.set("tile info out of range", tile); break; }
+    const std::vector<double> before(live, live + total);
     phase(sm, T, [&](double *buf, int t) { ptile::pxpass<N, K, T>(live, buf, &meta, nk, t); }, e, tile);
     phase(sm, T, [&](double *buf, int t) { ptile::pyzpass<N, K, T>(live, buf, &meta, nk, t); }, e, tile);
+    written_once(before, live, total, e, tile);
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
   }
   (void)total;
@@ -305,6 +316,7 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
       }
     }
     if (!e.ok) break;
+    const std::vector<double> before(live, live + total);
     // the kernel's choice: complete tiles take the passes' periodic form
     if (xtile::complete<OPEN>(&meta)) {
       phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, false, T>(buf, &meta, t); }, e, tile);
@@ -313,6 +325,7 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
       phase(sm, T, [&](double *buf, int t) { xtile::xxpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
       phase(sm, T, [&](double *buf, int t) { xtile::xyzpass<N, K, OPEN, T>(buf, &meta, t); }, e, tile);
     }
+    written_once(before, live, total, e, tile);
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
   }
   return e.ok ? 0 : -1;
