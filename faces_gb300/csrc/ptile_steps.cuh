@@ -205,100 +205,9 @@ __host__ __device__ __forceinline__ void pxpass(double *__restrict__ u, double *
   }
 }
 
-// two adjacent doubles at a 16-byte aligned address: one 16-byte access on
-// the device, two scalar ones in the host replay
-__host__ __device__ __forceinline__ double2 ld2(const double *p)
-{
-#ifdef __CUDA_ARCH__
-  return *reinterpret_cast<const double2 *>(p);
-#else
-  return make_double2(p[0], p[1]);
-#endif
-}
-
-__host__ __device__ __forceinline__ void st2(double *p, double2 v)
-{
-#ifdef __CUDA_ARCH__
-  *reinterpret_cast<double2 *>(p) = v;
-#else
-  p[0] = v.x;
-  p[1] = v.y;
-#endif
-}
-
-__host__ __device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-
-// pyzpass for even n: an item takes two adjacent points (x, x+1) of a
-// column pair, so that staged rows are read and final values stored 16 bytes
-// at a time (rows, staged rows and global rows all start on 16 bytes for
-// even n); the pair that holds the next chunk's seam (x+1 = n-1 of the last
-// element) stores only its first point.  The lower end column stays one
-// double per item.  Each lane's sums are the scalar pass's, in its order.
-template <int N, int K, int T>
-__host__ __device__ __forceinline__ void pyzpass_pairs(double *__restrict__ u, const double *buf, const PMeta *meta,
-                                                       int nk, int t)
-{
-  static_assert(N % 2 == 0, "pairs of points need even n");
-  constexpr int NN = N * N, RS = smem_row_stride(N), H = N / 2, PC = K * H;
-  constexpr long N3 = (long)N * N * N;
-  constexpr int G = 2 * (N - 2) + 1, COLS = PC + 1;
-  const double *locol = buf + K * NN * RS;
-  for (int i = t; i < G * COLS; i += T) {
-    const int g = i / COLS, c = i - g * COLS;
-    int ay = 0, az = 0, by = 0, bz = 0;
-    if (g < N - 2) { ay = N - 1; by = 0; az = bz = 1 + g; }                    // y pair
-    else if (g < 2 * (N - 2)) { ay = by = 1 + g - (N - 2); az = N - 1; bz = 0; }  // z pair
-    if (c < PC) {
-      const int k = c / H, x = 2 * (c - k * H);
-      if (k >= nk) continue;
-      const double *sb = buf + k * NN * RS + x;
-      const long gcol = k * N3 + x;
-      const bool half = k == nk - 1 && x == N - 2;  // x+1 is the next chunk's seam
-      auto put = [&](int sy, int sz, double2 v) {
-        double *p = u + meta->off[col_sel<N>(sy, sz)] + gcol + sz * NN + sy * N;
-        if (half) *p = v.x;
-        else st2(p, v);
-      };
-      if (g < 2 * (N - 2)) {
-        const double2 s = add2(ld2(sb + (az * N + ay) * RS), ld2(sb + (bz * N + by) * RS));
-        put(ay, az, s);
-        put(by, bz, s);
-      } else {
-        const double2 c00 = ld2(sb), c10 = ld2(sb + (N - 1) * RS);
-        const double2 c01 = ld2(sb + (N - 1) * N * RS), c11 = ld2(sb + (NN - 1) * RS);
-        const double2 s = add2(add2(c11, c01), add2(c10, c00));
-        put(0, 0, s);
-        put(N - 1, 0, s);
-        put(0, N - 1, s);
-        put(N - 1, N - 1, s);
-      }
-    } else {
-      auto gaddr = [&](int sy, int sz) { return u + meta->lo[col_sel<N>(sy, sz)] + (N - 1) + sz * NN + sy * N; };
-      if (g < 2 * (N - 2)) {
-        const double s = locol[az * N + ay] + locol[bz * N + by];
-        *gaddr(ay, az) = s;
-        *gaddr(by, bz) = s;
-      } else {
-        const double c00 = locol[0], c10 = locol[N - 1];
-        const double c01 = locol[(N - 1) * N], c11 = locol[NN - 1];
-        const double y0 = c10 + c00, y1 = c11 + c01;
-        const double s = y1 + y0;
-        *gaddr(0, 0) = s;
-        *gaddr(N - 1, 0) = s;
-        *gaddr(0, N - 1) = s;
-        *gaddr(N - 1, N - 1) = s;
-      }
-    }
-  }
-}
-
 template <int N, int K, int T = 256>
 __host__ __device__ __forceinline__ void pyzpass(double *__restrict__ u, const double *buf, const PMeta *meta, int nk, int t)
 {
-  if constexpr (N % 2 == 0) {
-    pyzpass_pairs<N, K, T>(u, buf, meta, nk, t);
-    return;
-  }
   constexpr int NN = N * N, RS = smem_row_stride(N);
   constexpr long N3 = (long)N * N * N;
   constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
