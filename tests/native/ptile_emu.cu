@@ -188,6 +188,7 @@ extern "C" int ptile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
                              int nsteps, char *err, int errlen)
 {
   Err e;
+  tiledev::host_misaligned_copies() = 0;
   const ReplayFn fn = pick(n, K, T);
   if (!fn || (T != 32 && T != 256)) {
     snprintf(err, errlen, "no replay for n = %d, K = %d, T = %d", n, K, T);
@@ -222,6 +223,7 @@ extern "C" int ptile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     fn(f, live.data() + kGuard, snap.data() + kGuard, total, p, e);
     if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
+    if (e.ok && tiledev::host_misaligned_copies() != 0) e.set("a 16-byte copy from or to an address not 16-byte aligned", -1);
     for (long i = 0; i < total && e.ok; i++) {
       const double v = live[kGuard + i];
       u[i] = std::isnan(v) ? snap[kGuard + i] : v;
@@ -382,6 +384,7 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
                              int messages, double *u, int nsteps, char *err, int errlen)
 {
   Err e;
+  tiledev::host_misaligned_copies() = 0;
   const XReplayFn fn = xpick(n, K, T, !periodic);
   if (!fn || (T != 32 && T != 256)) {
     snprintf(err, errlen, "no replay for n = %d, K = %d, T = %d", n, K, T);
@@ -426,6 +429,7 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     fn(f, live.data() + kGuard, snap.data() + kGuard, total, msg.data() + kGuard, msg_total, p, e);
     if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
+    if (e.ok && tiledev::host_misaligned_copies() != 0) e.set("a 16-byte copy from or to an address not 16-byte aligned", -1);
     if (e.ok && std::memcmp(msg.data(), msg_copy.data(), sizeof(double) * msg.size()) != 0)
       e.set("the step changed a message", -1);
     for (long i = 0; i < total && e.ok; i++) {
