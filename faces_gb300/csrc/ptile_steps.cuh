@@ -99,83 +99,6 @@ __host__ __device__ __forceinline__ void needed_piece(int j, int &sy, int &sz, i
   }
 }
 
-// The copies the periodic step issues per element.  Even n: as Needed (the
-// 16-byte pieces).  Odd n: a row is only 8-byte aligned, so it is staged at
-// shared offset ph in {0, 1} -- its global 16-byte phase: the parity of its
-// offset, (column offset + k + sy + sz) mod 2 since n^3, n^2 and n are odd --
-// which lines its doubles up with the shared stage's 16-byte grid.  A seam
-// row then moves in (n+1)/2 copies: with ph = 0 the pairs (0,1), (2,3), ...
-// and the last point alone, with ph = 1 the first point alone and the pairs
-// (1,2), (3,4), ...; an interior row moves its two end points.  Copy j of an
-// element -> row (sy, sz), copy index pc, interior or not.
-template <int N>
-struct Staged {
-  static constexpr int NP = N % 2 == 0 ? pieces_per_row(N) : (N + 1) / 2;  // copies per seam row
-  static constexpr int NI = (N - 2) * (N - 2), NB = N * N - NI;
-  static constexpr int E = N % 2 == 0 ? (NP > 1 ? 2 : 1) : 2;                // copies per interior row
-  static constexpr int count = NI * E + NB * NP;
-};
-
-template <int N>
-__host__ __device__ __forceinline__ void staged_copy(int j, int &sy, int &sz, int &pc, bool &interior)
-{
-  constexpr int NP = Staged<N>::NP, NI = Staged<N>::NI, E = Staged<N>::E;
-  interior = false;
-  if constexpr (NI > 0) {
-    if (j < NI * E) {
-      const int ri = j / E;
-      pc = j - ri * E;  // 0: the first piece or point, 1: the last
-      sy = 1 + ri % (N - 2);
-      sz = 1 + ri / (N - 2);
-      interior = true;
-      return;
-    }
-  }
-  j -= NI * E;
-  const int b = j / NP;
-  pc = j - b * NP;
-  if (b < N) { sy = b; sz = 0; }
-  else if (b < 2 * N) { sy = b - N; sz = N - 1; }
-  else {
-    const int t = b - 2 * N;
-    sz = 1 + t / 2;
-    sy = (t & 1) ? N - 1 : 0;
-  }
-}
-
-// copy pc of a row staged at phase ph: its first point x and length (1 or 2)
-template <int N>
-__host__ __device__ __forceinline__ void staged_span(bool interior, int pc, int ph, int &x, int &len)
-{
-  if constexpr (N % 2 == 0) {
-    x = interior ? (pc ? N - 2 : 0) : 2 * pc;
-    len = 2;
-  } else if (interior) {
-    x = pc ? N - 1 : 0;
-    len = 1;
-  } else if (ph == 0) {
-    x = 2 * pc;
-    len = x == N - 1 ? 1 : 2;
-  } else {
-    x = pc ? 2 * pc - 1 : 0;
-    len = pc ? 2 : 1;
-  }
-}
-
-// the shared-memory phase of row (sy, sz) of element k in a tile whose
-// column offsets have parities par (bit s: column s); 0 for even n
-template <int N>
-__host__ __device__ __forceinline__ int row_phase(int par, int k, int sy, int sz)
-{
-  if constexpr (N % 2 == 0) return 0;
-  return ((par >> col_sel<N>(sy, sz)) + k + sy + sz) & 1;
-}
-
-__host__ __device__ __forceinline__ int offset_parities(const long off[4])
-{
-  return (int)((off[0] & 1) | ((off[1] & 1) << 1) | ((off[2] & 1) << 2) | ((off[3] & 1) << 3));
-}
-
 // A team of T threads (a block of 256, or one warp) works on a tile; t is
 // the thread's index in its team.  The functions also compile for the host,
 // where tests/native/ptile_emu.cu replays them thread by thread.  Threads and needed slots: with more than
@@ -183,17 +106,17 @@ __host__ __device__ __forceinline__ int offset_parities(const long off[4])
 // every element of the tile; with fewer, KT = T/slots threads share a slot
 // and thread t takes its elements t/slots, +KT, ...  A thread decodes its
 // slot once per tile and walks the elements by adding the element stride.
-template <int N, int T, int COUNT = Needed<N>::count>
+template <int N, int T>
 struct PSlots {
-  static constexpr int NE = COUNT;
+  static constexpr int NE = Needed<N>::count;
   static constexpr int KT = NE <= T / 2 ? T / NE : 1;
   static constexpr int SPT = KT > 1 ? 1 : (NE + T - 1) / T;
 };
 
-template <int N, int T, int COUNT = Needed<N>::count>
+template <int N, int T>
 __host__ __device__ __forceinline__ bool pslot(int jj, int t, int &j, int &kq)
 {
-  constexpr int NE = PSlots<N, T, COUNT>::NE, KT = PSlots<N, T, COUNT>::KT;
+  constexpr int NE = PSlots<N, T>::NE, KT = PSlots<N, T>::KT;
   if constexpr (KT > 1) {
     j = t % NE;
     kq = t / NE;
@@ -213,8 +136,8 @@ __host__ __device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPl
   // one copy of the description (the batched kernel reads it from global
   // memory; stores through double pointers must not force it to reload)
   const FieldDesc f = fd;
-  constexpr int NN = N * N, RS = smem_row_stride(N), NC = Staged<N>::count;
-  constexpr int KT = PSlots<N, T, NC>::KT, SPT = PSlots<N, T, NC>::SPT;
+  constexpr int NN = N * N, PW = piece_doubles(N), RS = smem_row_stride(N);
+  constexpr int KT = PSlots<N, T>::KT, SPT = PSlots<N, T>::SPT;
   constexpr long N3 = (long)N * N * N;
   const int jx0 = u.c * p.chunk;
   const int nk = p.chunk < f.m[0] - jx0 ? p.chunk : f.m[0] - jx0;
@@ -231,21 +154,14 @@ __host__ __device__ __forceinline__ void pstage(const FieldDesc &fd, const RowPl
 #pragma unroll
   for (int jj = 0; jj < SPT; jj++) {
     int j, kq;
-    if (!pslot<N, T, NC>(jj, t, j, kq)) continue;
+    if (!pslot<N, T>(jj, t, j, kq)) continue;
     int sy, sz, pc;
-    bool interior;
-    staged_copy<N>(j, sy, sz, pc, interior);
+    needed_piece<N>(j, sy, sz, pc);
     const int s = col_sel<N>(sy, sz);
     const long o = s == 0 ? o0 : s == 1 ? o1 : s == 2 ? o2 : o3;
-    const double *g = f.u + o + kq * N3 + sz * NN + sy * N;  // the row's point 0
-    double *sp = buf + (kq * NN + sz * N + sy) * RS;
-    int ph = (N % 2) ? (int)((o + kq + sz + sy) & 1) : 0;
-    for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) {
-      int x, len;
-      staged_span<N>(interior, pc, ph, x, len);
-      cp_async(sp + ph + x, g + x, len);
-      if (N % 2) ph ^= KT & 1;
-    }
+    const double *g = f.u + o + kq * N3 + sz * NN + sy * N + pc * PW;
+    double *sp = buf + (kq * NN + sz * N + sy) * RS + pc * PW;
+    for (int k = kq; k < nk; k += KT, g += KT * N3, sp += KT * NN * RS) cp_async(sp, g, PW);
   }
   for (int r = t; r < NN; r += T) {
     const int sy = r % N, sz = r / N;
@@ -271,16 +187,14 @@ __host__ __device__ __forceinline__ void pxpass(double *__restrict__ u, double *
   constexpr long N3 = (long)N * N * N;
   double *locol = buf + K * NN * RS;
   const int items = nk * NN;
-  const int par = (N % 2) ? offset_parities(meta->off) : 0;
   for (int i = t; i < items; i += T) {
     const int k = i / NN, r = i - k * NN;
-    const int sy = r % N, sz = r / N;
-    const int ph = row_phase<N>(par, k, sy, sz);  // element k-1's row: the other phase (odd n)
-    double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (ph ^ (N % 2)) + (N - 1);
-    double *hi = buf + (k * NN + r) * RS + ph;
+    double *lo = k == 0 ? locol + r : buf + ((k - 1) * NN + r) * RS + (N - 1);
+    double *hi = buf + (k * NN + r) * RS;
     const double s = *lo + *hi;
     *lo = s;
     *hi = s;
+    const int sy = r % N, sz = r / N;
     if (sy >= 1 && sy <= N - 2 && sz >= 1 && sz <= N - 2) {
       // interior rows lie in column 0 (the tile's own elements)
       double *g = u + meta->off[0] + k * N3 + sz * NN + sy * N;
@@ -299,16 +213,14 @@ __host__ __device__ __forceinline__ void pyzpass(double *__restrict__ u, const d
   constexpr int G = 2 * (N - 2) + 1, COLS = K * N + 1;
   const double *locol = buf + K * NN * RS;
   const int last_c = (nk - 1) * N + (N - 1);  // the next chunk's seam: not stored
-  const int par = (N % 2) ? offset_parities(meta->off) : 0;
   for (int i = t; i < G * COLS; i += T) {
     const int g = i / COLS, c = i - g * COLS;
     const double *sb;
-    int srs, k = 0;
+    int srs;
     long gcol;  // offset of the column within its row, and which offsets table
     bool lo = false;
     if (c < K * N) {
-      k = c / N;
-      const int x = c - k * N;
+      const int k = c / N, x = c - k * N;
       if (k >= nk) continue;
       sb = buf + k * NN * RS + x;
       srs = RS;
@@ -322,20 +234,18 @@ __host__ __device__ __forceinline__ void pyzpass(double *__restrict__ u, const d
     const bool store = lo || c != last_c;
     const long *offs = lo ? meta->lo : meta->off;
     auto gaddr = [&](int sy, int sz) { return u + offs[col_sel<N>(sy, sz)] + gcol + sz * NN + sy * N; };
-    // the staged cell of row (sy, sz) at this column (odd n: at its phase)
-    auto cell = [&](int sy, int sz) { return sb[(sz * N + sy) * srs + (lo ? 0 : row_phase<N>(par, k, sy, sz))]; };
     if (g < 2 * (N - 2)) {
       int ay, az, by, bz;
       if (g < N - 2) { ay = N - 1; by = 0; az = bz = 1 + g; }              // y pair
       else { ay = by = 1 + g - (N - 2); az = N - 1; bz = 0; }              // z pair
-      const double s = cell(ay, az) + cell(by, bz);
+      const double s = sb[(az * N + ay) * srs] + sb[(bz * N + by) * srs];
       if (store) {
         *gaddr(ay, az) = s;
         *gaddr(by, bz) = s;
       }
     } else {
-      const double c00 = cell(0, 0), c10 = cell(N - 1, 0);
-      const double c01 = cell(0, N - 1), c11 = cell(N - 1, N - 1);
+      const double c00 = sb[0], c10 = sb[(N - 1) * srs];
+      const double c01 = sb[(N - 1) * N * srs], c11 = sb[(NN - 1) * srs];
       const double y0 = c10 + c00, y1 = c11 + c01;
       const double s = y1 + y0;
       if (store) {
