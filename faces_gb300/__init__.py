@@ -85,6 +85,8 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_tune.argtypes = [vp, c_int, c_int, c_int, c_int]
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
     L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip]
+    L.faces_batch_tune_warp.argtypes = [vp, c_int, c_int]
+    L.faces_batch_warp_info.argtypes = [vp, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
     jp, sp = ctypes.POINTER(FacesJob), ctypes.POINTER(ServeStats)
     llp, dblp = ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)
@@ -109,6 +111,7 @@ def lib() -> ctypes.CDLL:
                  "faces_run_host", "faces_set_tuning", "faces_launches_per_share", "faces_batch_create",
                  "faces_batch_add", "faces_batch_commit", "faces_batch_share", "faces_batch_share_n",
                  "faces_batch_share_each", "faces_batch_tune", "faces_batch_autotune", "faces_batch_info",
+                 "faces_batch_tune_warp", "faces_batch_warp_info",
                  "faces_batch_destroy"):
         getattr(L, name).restype = c_int
     _lib = L
@@ -376,6 +379,10 @@ class Batch:
     def tune(self, unit_div: int = 0, blocks_per_sm: int = 0, half: int = -1, run: int = 0) -> None:
         _check(lib().faces_batch_tune(self._h, unit_div, blocks_per_sm, half, run))
 
+    def tune_warp(self, max_n: int = -1, boost: int = 0) -> None:
+        """The warp form for small n (faces_batch_tune_warp)."""
+        _check(lib().faces_batch_tune_warp(self._h, max_n, boost))
+
     def autotune(self, trials: int = 3, stream=None) -> int:
         """Keeps the fastest work split; returns the shares it applied to
         each field of the batched launch (each timed launch is a share)."""
@@ -384,8 +391,12 @@ class Batch:
     def info(self) -> dict:
         v = [ctypes.c_int() for _ in range(7)]
         _check(lib().faces_batch_info(self._h, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks", "half", "run"),
-                        (x.value for x in v)))
+        out = dict(zip(("fields", "fused_fields", "units", "unit_div", "blocks", "half", "run"),
+                       (x.value for x in v)))
+        w = [ctypes.c_int() for _ in range(4)]
+        _check(lib().faces_batch_warp_info(self._h, *[ctypes.byref(x) for x in w]))
+        out.update(zip(("warp_max_n", "warp_boost", "warp_units", "warp_blocks"), (x.value for x in w)))
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None):

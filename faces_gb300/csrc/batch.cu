@@ -34,9 +34,14 @@ void faces_internal_set_error(const char *msg);
 namespace faces {
 
 
-RowPlan batch_plan(const FieldDesc &f, int half, bool lean)
+int batch_warp_chunk(int n) { return n >= kBatchMinN && n <= kBatchWarpMaxN ? bkw(n) : 0; }
+
+RowPlan batch_plan(const FieldDesc &f, int half, bool lean, bool warp)
 {
-  RowPlan p = make_row_plan(f, !batch_n_supported(f.n) ? 1 : lean ? bkl(f.n, half) : bk(f.n, half), 0);
+  const int k = !batch_n_supported(f.n) ? 1 : (warp && lean && half != 1 && batch_warp_chunk(f.n)) ? bkw(f.n)
+                : lean                                                                               ? bkl(f.n, half)
+                                                                                                     : bk(f.n, half);
+  RowPlan p = make_row_plan(f, k, 0);
   p.order = 2;
   p.unit_chunks = 1;
   return p;
@@ -73,16 +78,21 @@ void append_units(std::vector<BatchUnit> &units, int field, const RowPlan &p, in
 }
 
 cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int run,
-                         int mode, int half, cudaStream_t s)
+                         int mode, int half, cudaStream_t s, int nsmall, int wblocks)
 {
   if (run < 1) run = 1;
   if (nunits <= 0 || grid <= 0) return cudaSuccess;
   if (half && mode != 1) return cudaErrorInvalidValue;  // half-length tiles: periodic step only
-  if (mode == 1 && half == 2) return batch_launch_12(d_fields, d_units, nunits, grid, run, s);
-  if (mode == 1 && half) return batch_launch_11(d_fields, d_units, nunits, grid, run, s);
-  if (mode == 1) return batch_launch_10(d_fields, d_units, nunits, grid, run, s);
-  if (mode == 2) return batch_launch_20(d_fields, d_units, nunits, grid, run, s);
-  return batch_launch_00(d_fields, d_units, nunits, grid, run, s);
+  // the warp form: mode 1, stage forms 0 and 2, some blocks left for the
+  // other units unless there are none
+  if (nsmall < 0 || nsmall > nunits || wblocks < 0 || wblocks > grid) return cudaErrorInvalidValue;
+  if ((nsmall > 0) != (wblocks > 0) || (nsmall > 0 && (mode != 1 || half == 1))) return cudaErrorInvalidValue;
+  if (nsmall < nunits && wblocks >= grid) return cudaErrorInvalidValue;
+  if (mode == 1 && half == 2) return batch_launch_12(d_fields, d_units, nunits, grid, run, nsmall, wblocks, s);
+  if (mode == 1 && half) return batch_launch_11(d_fields, d_units, nunits, grid, run, nsmall, wblocks, s);
+  if (mode == 1) return batch_launch_10(d_fields, d_units, nunits, grid, run, nsmall, wblocks, s);
+  if (mode == 2) return batch_launch_20(d_fields, d_units, nunits, grid, run, nsmall, wblocks, s);
+  return batch_launch_00(d_fields, d_units, nunits, grid, run, nsmall, wblocks, s);
 }
 
 namespace {
@@ -124,6 +134,10 @@ struct faces_batch {
   int half = 0;      // tile length form (mode 1 only): 0 default, 1 half (4 blocks/SM), 2 long (2 blocks/SM)
   int unit_div = 2;  // units are 1/unit_div of a column's chunks
   int per_sm = 3;
+  int warp_n = kBatchWarpMaxN;  // fields with n up to this take the warp form (0: none)
+  int boost = 2;                // warp blocks: boost x their share of the points
+  int nsmall = 0;               // units of the warp form (listed first)
+  int wblocks = 0;              // blocks that run them
   int sms = 0;
   long grid = 0;
   cudaStream_t capture = nullptr;
@@ -144,10 +158,29 @@ void drop_graphs(faces_batch *b)
   b->graphs.clear();
 }
 
+// a batched field takes the warp form: every batched field on the periodic
+// step (mode 1), not the half-length stages, n up to warp_n
+bool warp_field(const faces_batch *b, const BatchField &bf)
+{
+  return b->mode == 1 && b->half != 1 && bf.lean && bf.f.n <= b->warp_n && batch_warp_chunk(bf.f.n) > 0;
+}
+
+// tile plans of every field for the current stage form and warp limit
+int plan_fields(faces_batch *b)
+{
+  for (size_t i = 0; i < b->h_fields.size(); i++)
+    b->h_fields[i].p = batch_plan(b->h_fields[i].f, b->half, b->h_fields[i].lean != 0, warp_field(b, b->h_fields[i]));
+  if (!b->h_fields.empty())
+    CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * b->h_fields.size(),
+                        cudaMemcpyHostToDevice),
+             "faces_batch: field table upload");
+  return FACES_OK;
+}
+
 int build_units(faces_batch *b)
 {
   // fields in order of n, so that the blocks resident at one time mostly run
-  // the code of one n
+  // the code of one n; the warp form's fields (the smallest n) come first
   std::vector<size_t> order;
   for (size_t i = 0; i < b->h_fields.size(); i++)
     if (b->fused[i]) order.push_back(i);
@@ -155,13 +188,38 @@ int build_units(faces_batch *b)
                    [&](size_t a, size_t c) { return b->h_fields[a].f.n < b->h_fields[c].f.n; });
   std::vector<BatchUnit> units;
   std::vector<BatchField> fused;
+  double small_pts = 0, large_pts = 0;
+  int nsmall = 0;
   for (size_t i : order) {
-    append_units(units, (int)i, b->h_fields[i].p, b->unit_div);
-    fused.push_back(b->h_fields[i]);
+    const BatchField &bf = b->h_fields[i];
+    const double pts = (double)bf.f.nranks * bf.f.m[0] * bf.f.m[1] * bf.f.m[2] * bf.f.n * bf.f.n * bf.f.n;
+    fused.push_back(bf);
+    if (warp_field(b, bf)) {
+      append_units(units, (int)i, bf.p, 1);  // whole columns
+      nsmall = (int)units.size();
+      small_pts += pts;
+    } else {
+      append_units(units, (int)i, bf.p, b->unit_div);
+      large_pts += pts;
+    }
   }
-  b->mode = batch_mode(fused.data(), fused.size());
   if (b->mode != 1 && b->half) return fail(FACES_EINVAL, "faces_batch: half-length tiles need all fields periodic");
-  b->grid = std::min<long>((long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half)), std::max(1, (int)units.size()));
+  const long G = (long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half));
+  const long nlarge = (long)units.size() - nsmall;
+  // blocks of the warp form: boost x the small fields' share of the points,
+  // at least one, and one or more left for the other units
+  long wb = 0;
+  if (nsmall > 0) {
+    wb = nlarge == 0 ? G
+                     : std::max(1L, std::min(G - 1, (long)(G * small_pts * b->boost / (small_pts * b->boost + large_pts) + 0.5)));
+    wb = std::min(wb, ((long)nsmall + 7) / 8);
+  }
+  b->nsmall = nsmall;
+  b->wblocks = (int)wb;
+  // blocks of the block pipeline: the rest, no more than its runs
+  const long runs = (nlarge + b->run - 1) / b->run;
+  b->grid = wb + std::max(nlarge > 0 ? 1L : 0L, std::min(G - wb, runs));
+  if (b->grid < 1) b->grid = 1;
   cudaFree(b->d_units);
   b->d_units = nullptr;
   b->nunits = (int)units.size();
@@ -170,29 +228,21 @@ int build_units(faces_batch *b)
     CUDA_TRY(cudaMemcpy(b->d_units, units.data(), sizeof(BatchUnit) * units.size(), cudaMemcpyHostToDevice),
              "faces_batch: work list upload");
   }
-  // blocks beyond the runs have nothing to do
-  const long runs = ((long)units.size() + b->run - 1) / b->run;
-  b->grid = std::max(1L, std::min(b->grid, runs));
   drop_graphs(b);
   return FACES_OK;
 }
 
-// tile plans of every field for full (0) or half-length (1) tiles
+// stage form: full (0), half-length (1) or long (2) tiles
 int set_half(faces_batch *b, int half)
 {
   b->half = half;
-  for (size_t i = 0; i < b->h_fields.size(); i++)
-    b->h_fields[i].p = batch_plan(b->h_fields[i].f, half, b->h_fields[i].lean != 0);
-  if (!b->h_fields.empty())
-    CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * b->h_fields.size(),
-                        cudaMemcpyHostToDevice),
-             "faces_batch: field table upload");
-  return FACES_OK;
+  return plan_fields(b);
 }
 
 int launch_batched(faces_batch *b, cudaStream_t s)
 {
-  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->run, b->mode, b->half, s),
+  CUDA_TRY(launch_batch(b->d_fields, b->d_units, b->nunits, b->grid, b->run, b->mode, b->half, s, b->nsmall,
+                        b->wblocks),
            "batch kernel launch");
   return FACES_OK;
 }
@@ -262,10 +312,13 @@ int faces_batch_commit(faces_batch *b)
     b->h_fields[i] = bf;
     b->fused[i] = batch_eligible(c) ? 1 : 0;
   }
+  std::vector<BatchField> fused;
+  for (size_t i = 0; i < nf; i++)
+    if (b->fused[i]) fused.push_back(b->h_fields[i]);
+  b->mode = batch_mode(fused.data(), fused.size());
   if (nf) {
     CUDA_TRY(cudaMalloc(&b->d_fields, sizeof(BatchField) * nf), "faces_batch: field table");
-    CUDA_TRY(cudaMemcpy(b->d_fields, b->h_fields.data(), sizeof(BatchField) * nf, cudaMemcpyHostToDevice),
-             "faces_batch: field table upload");
+    if (int rc = plan_fields(b)) return rc;
   }
   CUDA_TRY(batch_configure(), "faces_batch: shared memory attribute");
   b->per_sm = batch_blocks_per_sm(0);
@@ -381,15 +434,72 @@ int faces_batch_autotune(faces_batch *b, int trials, void *stream)
       pick = c;
     }
   }
+  if (rc == FACES_OK && pick.half != b->half) rc = set_half(b, pick.half);
+  if (rc == FACES_OK) {
+    b->unit_div = pick.div;
+    b->per_sm = pick.per_sm;
+    b->run = pick.run;
+    rc = build_units(b);
+  }
+  // then the warp form: which small n take it, and its share of the blocks
+  if (rc == FACES_OK && b->mode == 1 && b->half != 1) {
+    int best_n = b->warp_n, best_boost = b->boost;
+    best = 1e30f;
+    const int wns[] = {0, 3, 4, kBatchWarpMaxN};
+    const int boosts[] = {1, 2, 3, 4};
+    for (int wn : wns)
+      for (int bo : boosts) {
+        if (rc != FACES_OK || (wn == 0 && bo > 1)) continue;
+        b->warp_n = wn;
+        b->boost = bo;
+        if ((rc = plan_fields(b)) || (rc = build_units(b))) break;
+        if ((rc = launch_batched(b, s))) break;
+        cudaEventRecord(e0, s);
+        for (int t = 0; t < trials && rc == FACES_OK; t++) rc = launch_batched(b, s);
+        cudaEventRecord(e1, s);
+        applied += 1 + trials;
+        if (rc) break;
+        const cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+          rc = fail(FACES_ECUDA, "autotune: synchronize: %s", cudaGetErrorString(e));
+          break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+          best = ms;
+          best_n = wn;
+          best_boost = bo;
+        }
+      }
+    b->warp_n = best_n;
+    b->boost = best_boost;
+    if (rc == FACES_OK && (rc = plan_fields(b)) == FACES_OK) rc = build_units(b);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
-  if (pick.half != b->half && (rc = set_half(b, pick.half))) return rc;
-  b->unit_div = pick.div;
-  b->per_sm = pick.per_sm;
-  b->run = pick.run;
-  if ((rc = build_units(b))) return rc;
   return applied;
+}
+
+int faces_batch_tune_warp(faces_batch *b, int max_n, int boost)
+{
+  if (int rc = check_batch(b, true)) return rc;
+  if (max_n > kBatchWarpMaxN) return fail(FACES_EINVAL, "max_n = %d: at most %d", max_n, kBatchWarpMaxN);
+  if (max_n >= 0) b->warp_n = max_n;
+  if (boost > 0) b->boost = boost;
+  if (int rc = plan_fields(b)) return rc;
+  return build_units(b);
+}
+
+int faces_batch_warp_info(const faces_batch *b, int *max_n, int *boost, int *warp_units, int *warp_blocks)
+{
+  if (!b) return fail(FACES_EINVAL, "null batch");
+  if (max_n) *max_n = b->warp_n;
+  if (boost) *boost = b->boost;
+  if (warp_units) *warp_units = b->nsmall;
+  if (warp_blocks) *warp_blocks = b->wblocks;
+  return FACES_OK;
 }
 
 int faces_batch_info(const faces_batch *b, int *fields, int *fused_fields, int *units, int *unit_div, int *blocks,

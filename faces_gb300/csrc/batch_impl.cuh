@@ -67,6 +67,20 @@ __host__ __device__ constexpr bool bkl_fits(int n, int h)
 static_assert(bkl_fits(kBatchMinN, 0) && bkl_fits(kBatchMinN, 1) && bkl_fits(kBatchMinN, 2),
               "periodic-step tiles fit the stage");
 
+// The warp form for small n (periodic step, stage forms h = 0 and 2): each
+// of a block's 8 warps stages, sums and stores its own tiles in one eighth
+// of the data stages (kWarpStage doubles), without block barriers; tiles of
+// up to 32 elements that fill that share (n = 2: 32, 3: 18, 4: 10, 5: 6).
+constexpr int kWarpStage = (kBatchStages * kStage<0> / 8) & ~1;
+__host__ __device__ constexpr int bkw(int n)
+{
+  return (kWarpStage - 2 * n * n) / (n * n * smem_row_stride(n)) > 32
+             ? 32
+             : (kWarpStage - 2 * n * n) / (n * n * smem_row_stride(n));
+}
+static_assert(kStage<2> >= kStage<0>, "the warp form fits the long stages too");
+static_assert(bkw(kBatchWarpMaxN) >= 1, "warp tiles hold an element");
+
 // shared memory: data stages, then per-stage row arrays sized for n = 10
 constexpr long batch_smem_bytes(int h)
 {
@@ -105,7 +119,7 @@ __device__ __forceinline__ bool bwalk_run(int run, int nunits, int r, BWalk &w)
 }
 
 __device__ __forceinline__ void bwalk_next(const BatchField *fields, const BatchUnit *units, int nunits, int run,
-                                           BWalk &w)
+                                           int stride, BWalk &w)
 {
   if (w.c + 1 < w.c1) {
     w.c++;
@@ -113,7 +127,7 @@ __device__ __forceinline__ void bwalk_next(const BatchField *fields, const Batch
     return;
   }
   if (++w.u >= w.u_end) {
-    if (!bwalk_run(run, nunits, w.run_index + gridDim.x, w)) {
+    if (!bwalk_run(run, nunits, w.run_index + stride, w)) {
       w.done = true;
       return;
     }
@@ -204,14 +218,71 @@ __device__ __forceinline__ void bstage_any(int field, const BatchField &bf, cons
   }
 }
 
+// one tile of the warp form: stage, wait, x pairs, y/z pairs, by one warp
+template <int N>
+__device__ __forceinline__ void warp_tile(const BatchField *bf, const TileCursor &u, double *buf, PMeta *meta,
+                                          int4 *tinfo, int lane)
+{
+  constexpr int KW = bkw(N);
+  ptile::pstage<N, KW, 32>(bf->f, bf->p, u, buf, meta, tinfo, lane);
+  cp_wait<0>();
+  __syncwarp();
+  const int nk = tinfo->y;
+  ptile::pxpass<N, KW, 32>(meta->u, buf, meta, nk, lane);
+  __syncwarp();
+  ptile::pyzpass<N, KW, 32>(meta->u, buf, meta, nk, lane);
+  __syncwarp();
+}
+
+// Units [0, nsmall) are small-n fields' (periodic step, tiles of bkw(n)
+// elements): blocks [0, wblocks) take them, warp by warp (unit q: warp
+// q % (8 * wblocks) of the warp blocks).  The other blocks walk units
+// [nsmall, nunits) through the block pipeline.  MODE 1 only.
+template <int MODE, int H>
+__device__ __forceinline__ void warp_units(const BatchField *fields, const BatchUnit *units, int nsmall, int wblocks,
+                                           const Smem &m)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *buf = m.data + (long)warp * kWarpStage;
+  // the per-stage row arrays of the general step are unused here: they hold
+  // each warp's tile record
+  PMeta *meta = reinterpret_cast<PMeta *>(m.lop) + warp;
+  int4 *tinfo = reinterpret_cast<int4 *>(reinterpret_cast<PMeta *>(m.lop) + 8) + warp;
+  for (int q = blockIdx.x * 8 + warp; q < nsmall; q += wblocks * 8) {
+    const BatchUnit un = units[q];
+    const BatchField *bf = fields + un.field;
+    const int n = bf->f.n, nchunks = bf->p.nchunks;
+    TileCursor u = cursor_of(bf->p, (long)un.column * nchunks + un.c0);
+    for (int c = un.c0; c < un.c1; c++, u.c++) {
+      switch (n) {
+        case 2: warp_tile<2>(bf, u, buf, meta, tinfo, lane); break;
+        case 3: warp_tile<3>(bf, u, buf, meta, tinfo, lane); break;
+        case 4: warp_tile<4>(bf, u, buf, meta, tinfo, lane); break;
+        case 5: warp_tile<5>(bf, u, buf, meta, tinfo, lane); break;
+        default: break;
+      }
+    }
+  }
+}
+
 template <int MODE, int H>
 __global__ void __launch_bounds__(256, bblocks(H))
-    batch_kernel(const BatchField *fields, const BatchUnit *units, int nunits, int run)
+    batch_kernel(const BatchField *fields, const BatchUnit *units_all, int nunits_all, int run, int nsmall,
+                 int wblocks)
 {
   extern __shared__ __align__(16) double sm[];
   const Smem m = smem_layout<H>(sm);
+  if constexpr (MODE == 1 && H != 1) {
+    if ((int)blockIdx.x < wblocks) {
+      warp_units<MODE, H>(fields, units_all, nsmall, wblocks, m);
+      return;
+    }
+  }
+  // the block pipeline: units [nsmall, nunits_all), blocks [wblocks, grid)
+  const BatchUnit *units = units_all + nsmall;
+  const int nunits = nunits_all - nsmall, stride = (int)gridDim.x - wblocks;
   BWalk nw;  // next tile to stage
-  nw.done = !bwalk_run(run, nunits, blockIdx.x, nw);
+  nw.done = !bwalk_run(run, nunits, (int)blockIdx.x - wblocks, nw);
   if (nw.done) return;
   bwalk_unit(fields, units, nw);
   ColKey ck{};
@@ -228,7 +299,7 @@ __global__ void __launch_bounds__(256, bblocks(H))
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
       load_field(fields, nw.field, m.field + cur, cached_cur);
       bstage_any<MODE, H>(nw.field, m.field[cur], nw.cur, ck, have_col, col, m, j);
-      bwalk_next(fields, units, nunits, run, nw);
+      bwalk_next(fields, units, nunits, run, stride, nw);
       inflight++;
     } else {
       cp_commit();
@@ -250,7 +321,7 @@ __global__ void __launch_bounds__(256, bblocks(H))
     if (!nw.done) {
       if (nw.field != last_field) { have_col = false; last_field = nw.field; }
       bstage_any<MODE, H>(nw.field, m.field[cur], nw.cur, ck, have_col, col, m, sn);
-      bwalk_next(fields, units, nunits, run, nw);
+      bwalk_next(fields, units, nunits, run, stride, nw);
       inflight++;
       // the field of the tile staged next: already in a slot, or copied now
       // into the other slot, which nobody reads in this iteration (its last
@@ -319,9 +390,9 @@ cudaError_t batch_configure_t()
 
 template <int MODE, int H>
 cudaError_t batch_launch_t(const BatchField *fields, const BatchUnit *units, int nunits, long grid, int run,
-                           cudaStream_t s)
+                           int nsmall, int wblocks, cudaStream_t s)
 {
-  batch_kernel<MODE, H><<<(unsigned)grid, 256, batch_smem_bytes(H), s>>>(fields, units, nunits, run);
+  batch_kernel<MODE, H><<<(unsigned)grid, 256, batch_smem_bytes(H), s>>>(fields, units, nunits, run, nsmall, wblocks);
   return cudaGetLastError();
 }
 

@@ -6,9 +6,9 @@ namespace faces {
 cudaError_t batch_configure_20() { return batch_configure_t<2, 0>(); }
 
 cudaError_t batch_launch_20(const BatchField *fields, const BatchUnit *units, int nunits, long grid, int run,
-                            cudaStream_t s)
+                            int nsmall, int wblocks, cudaStream_t s)
 {
-  return batch_launch_t<2, 0>(fields, units, nunits, grid, run, s);
+  return batch_launch_t<2, 0>(fields, units, nunits, grid, run, nsmall, wblocks, s);
 }
 
 }  // namespace faces

@@ -13,6 +13,8 @@
 namespace faces {
 
 constexpr int kBatchMinN = 2, kBatchMaxN = 10;
+// the largest n the warp form of the batched kernel takes (batch_impl.cuh)
+constexpr int kBatchWarpMaxN = 5;
 
 struct BatchField {
   FieldDesc f;
@@ -30,8 +32,12 @@ inline bool batch_n_supported(int n) { return n >= kBatchMinN && n <= kBatchMaxN
 
 // the tile plan of a field in the batched kernel (half = 1: half-length
 // tiles, for the periodic-step form that keeps 4 blocks per SM); lean: the
-// field takes the periodic step, whose tiles fill the stage
-RowPlan batch_plan(const FieldDesc &f, int half, bool lean);
+// field takes the periodic step, whose tiles fill the stage; warp: the field
+// takes the warp form (periodic step, n <= kBatchWarpMaxN, half != 1)
+RowPlan batch_plan(const FieldDesc &f, int half, bool lean, bool warp = false);
+
+// tile length of the warp form for n
+int batch_warp_chunk(int n);
 
 // resident blocks per SM (3, or 4 with half-length tiles)
 int batch_blocks_per_sm(int half = 0);
@@ -48,9 +54,11 @@ int batch_mode(const BatchField *fields, size_t n);
 
 // one share of every field the units cover; blocks take runs of `run`
 // consecutive units (block b: runs b, b + grid, ...); half = 1 or 2 only with
-// mode 1 and plans from batch_plan(f, half)
+// mode 1 and plans from batch_plan(f, half).  The first nsmall units (warp-
+// form plans, mode 1, half != 1) go to blocks [0, wblocks), warp by warp;
+// the others to the remaining blocks.
 cudaError_t launch_batch(const BatchField *d_fields, const BatchUnit *d_units, int nunits, long grid, int run,
-                         int mode, int half, cudaStream_t s);
+                         int mode, int half, cudaStream_t s, int nsmall = 0, int wblocks = 0);
 
 // the kernel's forms, one translation unit each (batch_k<MODE><H>.cu):
 // MODE 0 general step, 1 periodic step, 2 each field its own; H the tile
@@ -60,10 +68,15 @@ cudaError_t batch_configure_20();
 cudaError_t batch_configure_10();
 cudaError_t batch_configure_11();
 cudaError_t batch_configure_12();
-cudaError_t batch_launch_00(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
-cudaError_t batch_launch_20(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
-cudaError_t batch_launch_10(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
-cudaError_t batch_launch_11(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
-cudaError_t batch_launch_12(const BatchField *, const BatchUnit *, int nunits, long grid, int run, cudaStream_t);
+cudaError_t batch_launch_00(const BatchField *, const BatchUnit *, int nunits, long grid, int run, int nsmall,
+                            int wblocks, cudaStream_t);
+cudaError_t batch_launch_20(const BatchField *, const BatchUnit *, int nunits, long grid, int run, int nsmall,
+                            int wblocks, cudaStream_t);
+cudaError_t batch_launch_10(const BatchField *, const BatchUnit *, int nunits, long grid, int run, int nsmall,
+                            int wblocks, cudaStream_t);
+cudaError_t batch_launch_11(const BatchField *, const BatchUnit *, int nunits, long grid, int run, int nsmall,
+                            int wblocks, cudaStream_t);
+cudaError_t batch_launch_12(const BatchField *, const BatchUnit *, int nunits, long grid, int run, int nsmall,
+                            int wblocks, cudaStream_t);
 
 }  // namespace faces

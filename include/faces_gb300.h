@@ -233,9 +233,23 @@ int faces_batch_share_each(faces_batch *b, int compute, void *stream);
  * (units a block takes in a row before striding by the grid; <= 0 keeps it). */
 int faces_batch_tune(faces_batch *b, int unit_div, int blocks_per_sm, int half, int run);
 
+/* The warp form of the batched launch (every batched field periodic, stage
+ * form 0 or 2): fields with n <= max_n (at most 5; 0: none; < 0 keeps it)
+ * are cut into whole-column units that the first blocks of the launch take
+ * warp by warp -- each warp stages, sums and stores its own tiles, with no
+ * block barrier -- while the other blocks run the block pipeline over the
+ * rest; those first blocks are `boost` (<= 0 keeps it) times the small
+ * fields' share of the points, of all blocks.  Default: max_n 5, boost 2. */
+int faces_batch_tune_warp(faces_batch *b, int max_n, int boost);
+
+/* The warp form's max_n and boost, its units and its blocks (each may be
+ * NULL). */
+int faces_batch_warp_info(const faces_batch *b, int *max_n, int *boost, int *warp_units, int *warp_blocks);
+
 /* Times the batched launch over unit_div in {1,2,4,8,64}, the tile lengths
  * (when allowed), runs of 1 or 8 units per block and the resident blocks per SM that fit, `trials` launches each (after one warm-up), and
- * keeps the fastest.  Every launch is a share of the fields in the batched
+ * keeps the fastest; then, with those, the warp form's max_n in {0,3,4,5}
+ * and boost in {1,2,3,4}.  Every launch is a share of the fields in the batched
  * launch (the others are untouched): returns how many shares it applied to
  * each of them (>= 0), or a negative error code.  Synchronous. */
 int faces_batch_autotune(faces_batch *b, int trials, void *stream);

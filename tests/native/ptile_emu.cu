@@ -152,9 +152,11 @@ ReplayFn pick_k(int K, int T)
     case 6: return pick_t<N, 6>(T);
     case 8: return pick_t<N, 8>(T);
     case 9: return pick_t<N, 9>(T);
+    case 10: return pick_t<N, 10>(T);
     case 12: return pick_t<N, 12>(T);
     case 16: return pick_t<N, 16>(T);
     case 17: return pick_t<N, 17>(T);
+    case 18: return pick_t<N, 18>(T);
     case 27: return pick_t<N, 27>(T);
     case 32: return pick_t<N, 32>(T);
     default: return nullptr;

@@ -184,3 +184,40 @@ def test_half_tiles_need_periodic_fields(faces_lib):
     b.close()
     for f, _ in fields:
         f.close()
+
+
+# periodic fields only (the warp form needs every batched field on the
+# periodic step): small n for the warp form, larger n for the block pipeline
+WARP_MIX = [((1, 1, 1, m[0], m[1], m[2], n), True, False) for m, n in (
+    ((3, 2, 4), 2), ((5, 3, 2), 3), ((24, 2, 3), 3), ((1, 1, 1), 3), ((7, 4, 4), 4), ((11, 2, 5), 4),
+    ((13, 3, 2), 5), ((6, 6, 6), 5), ((2, 9, 2), 5), ((4, 3, 5), 6), ((9, 2, 2), 7), ((3, 4, 3), 8),
+    ((2, 2, 7), 10))] + [((2, 1, 2, 3, 2, 2, 4), True, False), ((1, 2, 1, 7, 2, 3, 5), True, False)]
+
+
+@pytest.mark.parametrize("warp", [(0, 1), (3, 1), (5, 2), (5, 4), (4, 3)], ids=lambda w: f"max_n{w[0]}-boost{w[1]}")
+@pytest.mark.parametrize("half", [0, 2])
+def test_warp_form_equals_alone(oracle, faces_lib, warp, half):
+    """Small-n fields taken warp by warp in the same launch as the block
+    pipeline: every field as alone and as the oracle gives it, bit for bit."""
+    O, F = oracle, faces_lib
+    exp = alone(F, WARP_MIX, 3)
+    fields = make_fields(F, WARP_MIX)
+    b = F.Batch()
+    for f, u in fields:
+        b.add(f, u)
+    b.commit()
+    b.tune(0, 0, half, 0)
+    b.tune_warp(*warp)
+    info = b.info()
+    assert info["warp_max_n"] == warp[0]
+    assert (info["warp_units"] > 0) == (warp[0] >= 2)
+    b.share_n(3)
+    torch.cuda.synchronize()
+    for i, ((f, u), e) in enumerate(zip(fields, exp)):
+        assert np.array_equal(u.cpu().numpy(), e), f"field {i} {WARP_MIX[i][0]}"
+    sh = WARP_MIX[6][0]
+    s = O.Shape(*sh, periodic=True)
+    assert np.array_equal(fields[6][1].cpu().numpy(), O.groups_share(s, O.init_int(s, 17), True, 3))
+    b.close()
+    for f, _ in fields:
+        f.close()

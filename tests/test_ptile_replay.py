@@ -51,6 +51,12 @@ def batch_tile(n, stage=2688):
     return min(32, (stage - 2 * n * n) // (n * n * row_stride(n)))
 
 
+def batch_warp_tile(n, stage=2688):
+    """the batched kernel's warp form: one eighth of three default stages"""
+    w = (3 * stage // 8) & ~1
+    return min(32, (w - 2 * n * n) // (n * n * row_stride(n)))
+
+
 def tile_kwarp(n):
     """the warp form's tile length (about 6 KB of stage)"""
     v = 6144 // (n * n * row_stride(n) * 8)
@@ -63,7 +69,7 @@ def cases():
         ks = sorted({1, 2, tile_kmax(n)} | ({batch_tile(n)} if n <= 10 else set()))
         for K in ks:
             out.append((n, K, 256))
-        for K in sorted({tile_kmax(n), tile_kwarp(n)}):
+        for K in sorted({tile_kmax(n), tile_kwarp(n)} | ({batch_warp_tile(n)} if n <= 5 else set())):
             out.append((n, K, 32))
     return out
 
@@ -85,6 +91,11 @@ def test_ptile_replay_matches_oracle(oracle, n, K, T, grid):
     assert rc == 0, err.value.decode()
     exp = O.groups_share(s, u0.copy(), True, 2)
     assert np.array_equal(u, exp), f"{np.count_nonzero(u != exp)} points differ"
+
+
+def test_batch_warp_tile_lengths():
+    """the warp form's lengths replayed above (n = 2: 32, 3: 18, 4: 10, 5: 6)"""
+    assert [batch_warp_tile(n) for n in range(2, 6)] == [32, 18, 10, 6]
 
 
 def test_batch_tile_lengths():
