@@ -586,7 +586,8 @@ def served_leg(F) -> dict:
     shares = sum(j.nshares for j in jobs)
     pts = sum(j.lx * j.ly * j.lz * j.mx * j.my * j.mz * j.n ** 3 * j.nshares for j in jobs)
     runs = []
-    for plain, rates in ((False, (float("inf"), 1000.0, 500.0)), (True, (float("inf"), 1000.0))):
+    for plain, rates in ((False, (float("inf"), 2000.0, 1000.0, 500.0, 250.0)),
+                         (True, (float("inf"), 2000.0, 1000.0, 500.0, 250.0))):
         for rate in rates:
             rng = np.random.default_rng(7)
             arr = (np.zeros(len(jobs)) if rate == float("inf")
@@ -603,6 +604,8 @@ def served_leg(F) -> dict:
                          "makespan_s": round(mk, 4), "ticks": st["ticks"], "launches": st["launches"],
                          "peak_resident_gb": round(st["peak_resident_bytes"] / 1e9, 3)})
     sat = {r["form"]: r["steps_per_s"] for r in runs if r["rate_jobs_per_s"] is None}
+    curve = {form: [(r["rate_jobs_per_s"] or "inf", r["steps_per_s"], r["p50_ms"], r["p99_ms"]) for r in runs
+                    if r["form"] == form] for form in ("batched", "plain")}
     return {
         "workload": f"{len(jobs)} jobs: rank grid in {{1,2}}^3, m per dimension log-uniform in [2,32], n uniform in "
                     "{4..8}, 10..200 shares, periodic, integer fields; Poisson arrivals (rate inf = all at t=0)",
@@ -610,6 +613,7 @@ def served_leg(F) -> dict:
         "steps": "job shares (one share of one job)",
         "runs": runs,
         "speedup_vs_plain_saturated": round(sat["batched"] / sat["plain"], 3),
+        "curve": {"columns": ["rate jobs/s", "job-steps/s", "p50 ms", "p99 ms"], **curve},
         "latency": "arrival to GPU completion of the job's last share",
     }
 

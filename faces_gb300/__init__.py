@@ -86,6 +86,7 @@ def lib() -> ctypes.CDLL:
     L.faces_batch_autotune.argtypes = [vp, c_int, vp]
     L.faces_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, ip, ip]
     L.faces_batch_tune_warp.argtypes = [vp, c_int, c_int]
+    L.faces_server_tune_warp.argtypes = [vp, c_int, c_int]
     L.faces_batch_warp_info.argtypes = [vp, ip, ip, ip, ip]
     L.faces_batch_destroy.argtypes = [vp]
     jp, sp = ctypes.POINTER(FacesJob), ctypes.POINTER(ServeStats)
@@ -104,7 +105,8 @@ def lib() -> ctypes.CDLL:
     L.faces_server_tune.argtypes = [vp, c_int, c_int, c_int]
     for name in ("faces_server_create", "faces_server_submit", "faces_server_poll", "faces_server_drain",
                  "faces_server_job_status", "faces_server_field", "faces_server_fetch", "faces_server_release",
-                 "faces_server_stats", "faces_server_run_trace", "faces_server_destroy", "faces_server_tune"):
+                 "faces_server_stats", "faces_server_run_trace", "faces_server_destroy", "faces_server_tune",
+                 "faces_server_tune_warp"):
         getattr(L, name).restype = c_int
     for name in ("faces_create", "faces_destroy", "faces_layout", "faces_field_alloc", "faces_field_free",
                  "faces_share", "faces_share_n", "faces_init_ref", "faces_init_int", "faces_check",
@@ -478,6 +480,10 @@ class Server:
     def tune(self, unit_div: int = 0, run: int = 0, half: int = -1) -> None:
         """Work list settings of the batched launch (faces_server_tune)."""
         _check(lib().faces_server_tune(self._h, unit_div, run, half))
+
+    def tune_warp(self, max_n: int = -1, boost: int = 0) -> None:
+        """The warp form for small n (faces_server_tune_warp)."""
+        _check(lib().faces_server_tune_warp(self._h, max_n, boost))
 
     def stats(self) -> dict:
         st = ServeStats()

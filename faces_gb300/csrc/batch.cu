@@ -36,6 +36,22 @@ namespace faces {
 
 int batch_warp_chunk(int n) { return n >= kBatchMinN && n <= kBatchWarpMaxN ? bkw(n) : 0; }
 
+void warp_split(long G, int nsmall, long nlarge, double small_pts, double large_pts, int boost, int run,
+                int &wblocks, long &grid)
+{
+  long wb = 0;
+  if (nsmall > 0) {
+    wb = nlarge == 0 ? G
+                     : std::max(1L, std::min(G - 1, (long)(G * small_pts * boost / (small_pts * boost + large_pts) + 0.5)));
+    wb = std::min(wb, ((long)nsmall + 7) / 8);  // 8 warps a block
+  }
+  wblocks = (int)wb;
+  // blocks of the block pipeline: the rest, no more than its runs
+  const long runs = (nlarge + std::max(1, run) - 1) / std::max(1, run);
+  grid = wb + std::max(nlarge > 0 ? 1L : 0L, std::min(G - wb, runs));
+  if (grid < 1) grid = 1;
+}
+
 RowPlan batch_plan(const FieldDesc &f, int half, bool lean, bool warp)
 {
   const int k = !batch_n_supported(f.n) ? 1 : (warp && lean && half != 1 && batch_warp_chunk(f.n)) ? bkw(f.n)
@@ -205,21 +221,8 @@ int build_units(faces_batch *b)
   }
   if (b->mode != 1 && b->half) return fail(FACES_EINVAL, "faces_batch: half-length tiles need all fields periodic");
   const long G = (long)b->sms * std::min(b->per_sm, batch_blocks_per_sm(b->half));
-  const long nlarge = (long)units.size() - nsmall;
-  // blocks of the warp form: boost x the small fields' share of the points,
-  // at least one, and one or more left for the other units
-  long wb = 0;
-  if (nsmall > 0) {
-    wb = nlarge == 0 ? G
-                     : std::max(1L, std::min(G - 1, (long)(G * small_pts * b->boost / (small_pts * b->boost + large_pts) + 0.5)));
-    wb = std::min(wb, ((long)nsmall + 7) / 8);
-  }
   b->nsmall = nsmall;
-  b->wblocks = (int)wb;
-  // blocks of the block pipeline: the rest, no more than its runs
-  const long runs = (nlarge + b->run - 1) / b->run;
-  b->grid = wb + std::max(nlarge > 0 ? 1L : 0L, std::min(G - wb, runs));
-  if (b->grid < 1) b->grid = 1;
+  warp_split(G, nsmall, (long)units.size() - nsmall, small_pts, large_pts, b->boost, b->run, b->wblocks, b->grid);
   cudaFree(b->d_units);
   b->d_units = nullptr;
   b->nunits = (int)units.size();

@@ -39,6 +39,14 @@ RowPlan batch_plan(const FieldDesc &f, int half, bool lean, bool warp = false);
 // tile length of the warp form for n
 int batch_warp_chunk(int n);
 
+// The launch of a work list whose first nsmall units take the warp form:
+// G the blocks that fit, nlarge the other units, *_pts the points of each
+// part, boost the warp blocks' weight, run the block pipeline's run length.
+// Sets the warp blocks (boost x their share of the points, at least one,
+// one or more left for the other units) and the whole grid.
+void warp_split(long G, int nsmall, long nlarge, double small_pts, double large_pts, int boost, int run,
+                int &wblocks, long &grid);
+
 // resident blocks per SM (3, or 4 with half-length tiles)
 int batch_blocks_per_sm(int half = 0);
 

@@ -122,6 +122,8 @@ struct faces_server {
   int nunits = 0;
   int kmode = 0, khalf = 0;  // kernel form of the running set's work list
   int unit_div = kServeUnitDiv, run = kServeRun, half = 0;  // work list settings (faces_server_tune)
+  int warp_n = kBatchWarpMaxN, boost = 2;  // the warp form (faces_server_tune_warp)
+  int nsmall = 0, wblocks = 0;
   long grid = 0;
   Tick ticks[kDepth];
   int tick_head = 0, in_flight = 0;  // ring of in-flight ticks
@@ -300,14 +302,28 @@ int rebuild_tables(faces_server *s, Tick &t)
   std::vector<BatchField> fields;
   std::vector<BatchUnit> units;
   fields.reserve(order.size());
+  // jobs of small n (the smallest, so listed first) take the warp form when
+  // every job is on the periodic step
+  int nsmall = 0;
+  double small_pts = 0, large_pts = 0;
   for (long long id : order) {
     const Job &job = s->jobs[id];
-    const RowPlan p = batch_plan(job.f, half, ptile_field(job.f));
-    append_units(units, (int)fields.size(), p, s->unit_div);
+    const bool warp = kmode == 1 && half != 1 && job.f.n <= s->warp_n && batch_warp_chunk(job.f.n) > 0;
+    const RowPlan p = batch_plan(job.f, half, ptile_field(job.f), warp);
+    append_units(units, (int)fields.size(), p, warp ? 1 : s->unit_div);
     fields.push_back({job.f, p, ptile_field(job.f) ? 1 : 0});
+    const double pts = (double)job.f.nranks * job.f.m[0] * job.f.m[1] * job.f.m[2] * job.f.n * job.f.n * job.f.n;
+    if (warp) {
+      nsmall = (int)units.size();
+      small_pts += pts;
+    } else {
+      large_pts += pts;
+    }
   }
-  const long runs = ((long)units.size() + s->run - 1) / s->run;
-  const long grid = std::max(1L, std::min<long>((long)s->sms * batch_blocks_per_sm(half), runs));
+  int wblocks = 0;
+  long grid = 0;
+  warp_split((long)s->sms * batch_blocks_per_sm(half), nsmall, (long)units.size() - nsmall, small_pts, large_pts,
+             s->boost, s->run, wblocks, grid);
   const size_t fbytes = (fields.size() * sizeof(BatchField) + 255) / 256 * 256;
   const size_t ubytes = units.size() * sizeof(BatchUnit);
   const size_t bytes = fbytes + ubytes;
@@ -332,6 +348,8 @@ int rebuild_tables(faces_server *s, Tick &t)
   s->kmode = kmode;
   s->khalf = half;
   s->nunits = (int)units.size();
+  s->nsmall = nsmall;
+  s->wblocks = wblocks;
   s->grid = grid;
   s->set_changed = false;
   return FACES_OK;
@@ -353,7 +371,7 @@ int launch_tick(faces_server *s)
       if (int rc = rebuild_tables(s, t)) return rc;
     CUDA_TRY(launch_batch(reinterpret_cast<const BatchField *>(s->d_tables),
                           reinterpret_cast<const BatchUnit *>(s->d_tables + s->tables_fbytes), s->nunits, s->grid,
-                          s->run, s->kmode, s->khalf, s->stream),
+                          s->run, s->kmode, s->khalf, s->stream, s->nsmall, s->wblocks),
              "server: batched launch");
     s->launches++;
   }
@@ -547,6 +565,16 @@ int faces_server_tune(faces_server *s, int unit_div, int run, int half)
   if (half >= 0) s->half = half;
   if (unit_div > 0) s->unit_div = unit_div;
   if (run > 0) s->run = run;
+  s->set_changed = true;
+  return FACES_OK;
+}
+
+int faces_server_tune_warp(faces_server *s, int max_n, int boost)
+{
+  if (!s) return fail(FACES_EINVAL, "null server");
+  if (max_n > kBatchWarpMaxN) return fail(FACES_EINVAL, "max_n = %d: at most %d", max_n, kBatchWarpMaxN);
+  if (max_n >= 0) s->warp_n = max_n;
+  if (boost > 0) s->boost = boost;
   s->set_changed = true;
   return FACES_OK;
 }

@@ -340,6 +340,12 @@ int faces_server_stats(const faces_server *s, faces_serve_stats *st);
  * Values <= 0 (half < 0) keep the setting. */
 int faces_server_tune(faces_server *s, int unit_div, int run, int half);
 
+/* The warp form of the server's batched launch, as faces_batch_tune_warp:
+ * jobs with n <= max_n (at most 5; 0: none; < 0 keeps it) are taken warp by
+ * warp by the first blocks, `boost` (<= 0 keeps it) times their share of the
+ * points.  Default: max_n 5, boost 2.  Applies from the next tick. */
+int faces_server_tune_warp(faces_server *s, int max_n, int boost);
+
 /* Replays an arrival trace in real time: job i is submitted when
  * arrival_s[i] seconds (non-decreasing) have passed since the call began,
  * stamped with that time, and the call returns when all are done.
