@@ -639,6 +639,21 @@ def profile_c4(F, shares: int) -> dict:
     return {"case": "c4", "shares": shares, "batch": b.info()}
 
 
+def profile_c3(F, mode: str, shares: int) -> dict:
+    """The C3 grid (3x3x3 periodic ranks of 16^3 elements, n=6) in one mode,
+    default settings, `shares` shares one call at a time: the case the C3
+    kernels are profiled on."""
+    import torch
+    f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6")
+    u = f.field()
+    f.init_int(u, SEED)
+    for _ in range(shares):
+        f.share(u)
+    torch.cuda.synchronize()
+    chk = f.check(u, init="int", seed=SEED, nshares=shares)
+    return {"case": "c3", "mode": mode, "shares": shares, "tuning": f.tuning(), "check_passed": bool(chk.passed)}
+
+
 def run_reference(args) -> dict | None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -677,11 +692,18 @@ def main() -> None:
                     help="set the tile settings instead of autotuning (profiling runs)")
     ap.add_argument("--profile-c4", type=int, default=0, metavar="N",
                     help="only build the 512-field batch and run N batched shares (for ncu)")
+    ap.add_argument("--profile-c3", default="", metavar="MODE,N",
+                    help="only run N shares of the C3 grid in MODE (messages, direct, v6) (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_c4:
         import faces_gb300 as F
         print(json.dumps(profile_c4(F, args.profile_c4)), flush=True)
+        return
+    if args.profile_c3:
+        import faces_gb300 as F
+        mode, n = args.profile_c3.split(",")
+        print(json.dumps(profile_c3(F, mode, int(n))), flush=True)
         return
     out = run_reference(args) if args.impl == "reference" else run_faces(args)
     if out is not None:
