@@ -24,7 +24,8 @@ cpu_baseline = the reference's v-26 pack/inner/unpack loops transcribed to
 
 c3       = 3x3x3 periodic virtual ranks of 16^3 elements, n=6: 26 messages
             per rank packed, swapped by buffer and unpack-added (v-26), with
-            direct mode and v-6 beside it; GB/s over field and message bytes
+            direct mode, v-6 and fused v-6 beside it; GB/s over field and
+            message bytes
 reference_gpu = the reference's own CUDA build (gpu/main.cc + v-26 Faces.cc,
             one-rank MPI stand-in, built by baseline/Makefile where its
             sources are staged) against this repository's `faces` executable
@@ -416,11 +417,11 @@ def c3_leg(F, dev) -> dict:
     stream = torch.cuda.current_stream(dev)
     peak, peak_kind = hbm_peak()
     modes = {}
-    for mode in ("messages", "direct", "v6"):
-        f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6")
+    for mode in ("messages", "direct", "v6", "v6f"):
+        f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6", v6f=mode == "v6f")
         u = f.field(dev)
         f.init_int(u, SEED, stream)
-        if mode != "v6":
+        if not mode.startswith("v6"):
             f.autotune(u, True, 3, stream)
         f.init_int(u, SEED, stream)
         for _ in range(3):
@@ -428,7 +429,7 @@ def c3_leg(F, dev) -> dict:
         f.init_int(u, SEED, stream)
         ms = _events_ms(lambda: f.share_n(u, C3_STEPS, True, stream), stream, 1) / C3_STEPS
         chk = f.check(u, init="int", seed=SEED, nshares=C3_STEPS)
-        msg = 0 if mode == "direct" else c3_message_doubles(C3_SHAPE, mode == "v6")
+        msg = 0 if mode == "direct" else c3_message_doubles(C3_SHAPE, mode.startswith("v6"))
         b = 16 * (f.points + msg)
         modes[mode] = {"ms_per_share": round(ms, 5), "gbs": round(b / (ms * 1e-3) / 1e9, 1),
                        "field_gbs": round(16 * f.points / (ms * 1e-3) / 1e9, 1),
@@ -644,7 +645,7 @@ def profile_c3(F, mode: str, shares: int) -> dict:
     default settings, `shares` shares one call at a time: the case the C3
     kernels are profiled on."""
     import torch
-    f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6")
+    f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6", v6f=mode == "v6f")
     u = f.field()
     f.init_int(u, SEED)
     for _ in range(shares):
@@ -693,7 +694,7 @@ def main() -> None:
     ap.add_argument("--profile-c4", type=int, default=0, metavar="N",
                     help="only build the 512-field batch and run N batched shares (for ncu)")
     ap.add_argument("--profile-c3", default="", metavar="MODE,N",
-                    help="only run N shares of the C3 grid in MODE (messages, direct, v6) (for ncu)")
+                    help="only run N shares of the C3 grid in MODE (messages, direct, v6, v6f) (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile_c4:

@@ -28,6 +28,7 @@ GATHER = 0x4
 ROWS = 0x8
 GENERAL = 0x10
 V6 = 0x20
+V6F = 0x40
 
 _ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
 
@@ -207,19 +208,21 @@ class Faces:
     general  -- periodic fields: the general tile step instead of the periodic one
     v6       -- v-6 strategy: six face messages per rank, sweeps z, y, x
                 (gpu/v-6-messages-basic/Faces.cc:65-173)
+    v6f      -- v-6 in the fused form of gpu/v-6-messages-overlap-fusable/
+                Faces.cc: four launches per share, the same results as v6
     """
 
     def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
                  periodic: bool = False, messages: bool = False, gather: bool = False, rows: bool = False,
-                 general: bool = False, v6: bool = False):
+                 general: bool = False, v6: bool = False, v6f: bool = False):
         flags = ((PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
-                 | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0))
+                 | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0) | (V6F if v6f else 0))
         h = ctypes.c_void_p()
         _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
         self._h = h
         self.shape = (lx, ly, lz, mx, my, mz, n)
         self.periodic, self.messages, self.gather, self.rows = periodic, messages, gather, rows
-        self.general, self.v6 = general, v6
+        self.general, self.v6, self.v6f = general, v6, v6f
         s = (ctypes.c_long * 6)()
         rd, tot = ctypes.c_long(), ctypes.c_long()
         _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
@@ -360,7 +363,7 @@ class Batch:
         lx, ly, lz, mx, my, mz, n = faces.shape
         flags = ((PERIODIC if faces.periodic else 0) | (MESSAGES if faces.messages else 0)
                  | (GATHER if faces.gather else 0) | (ROWS if faces.rows else 0)
-                 | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0))
+                 | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0) | (V6F if faces.v6f else 0))
         fid = ctypes.c_int()
         _check(lib().faces_batch_add(self._h, _ptr(u), lx, ly, lz, mx, my, mz, n, flags, ctypes.byref(fid)))
         self._fields.append(u)

@@ -165,7 +165,8 @@ namespace {
 
 bool batch_eligible(const faces_ctx *c)
 {
-  return batch_n_supported(c->n) && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS));
+  // message strategies keep their own order of sums: one faces_share each
+  return batch_n_supported(c->n) && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F));
 }
 
 void drop_graphs(faces_batch *b)

@@ -138,10 +138,10 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   if (lx < 1 || ly < 1 || lz < 1) return fail(FACES_EINVAL, "rank grid %d x %d x %d must be positive", lx, ly, lz);
   if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
   if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
-  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL | FACES_V6))
+  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL | FACES_V6 | FACES_V6F))
     return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
-  if ((flags & FACES_V6) && (flags & FACES_MESSAGES))
-    return fail(FACES_EINVAL, "FACES_V6 and FACES_MESSAGES are two message strategies: choose one");
+  if (((flags & FACES_V6) != 0) + ((flags & FACES_V6F) != 0) + ((flags & FACES_MESSAGES) != 0) > 1)
+    return fail(FACES_EINVAL, "FACES_V6, FACES_V6F and FACES_MESSAGES are message strategies: choose one");
   const long nranks = (long)lx * ly * lz;
   if (nranks > 65535 / 27) return fail(FACES_EINVAL, "%ld ranks: at most %d virtual ranks", nranks, 65535 / 27);
   faces_ctx *c = new (std::nothrow) faces_ctx();
@@ -158,7 +158,7 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   c->nbr = neighbour_table(c->L, (flags & FACES_PERIODIC) != 0);
   c->msg_off.assign(nranks * 27, -1);
   if (flags & FACES_MESSAGES) c->msg_total = message_offsets(c->desc(nullptr), c->nbr, c->msg_off);
-  if (flags & FACES_V6) c->msg_total = v6_message_doubles(c->desc(nullptr));
+  if (flags & (FACES_V6 | FACES_V6F)) c->msg_total = v6_message_doubles(c->desc(nullptr));
   c->recv_off = receive_offsets(c->nbr, c->msg_off);
   cudaError_t e;
   if ((e = cudaMalloc(&c->d_nbr, sizeof(int) * nranks * 27)) != cudaSuccess ||
@@ -269,6 +269,7 @@ int faces_launches_per_share(const faces_ctx *c, int compute)
   if (int rc = check_ctx(c)) return rc;
   (void)compute;
   if (c->flags & FACES_V6) return 6;
+  if (c->flags & FACES_V6F) return 4;
   return (c->flags & FACES_MESSAGES) ? 2 : 1;
 }
 
@@ -277,6 +278,10 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   const FieldDesc f = c->desc(u);
   if (c->flags & FACES_V6) {
     CUDA_TRY(launch_v6(f, c->d_msg, compute, s), "v-6 kernel launch");
+    return FACES_OK;
+  }
+  if (c->flags & FACES_V6F) {
+    CUDA_TRY(launch_v6_fused(f, c->d_msg, compute, s), "fused v-6 kernel launch");
     return FACES_OK;
   }
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
@@ -315,7 +320,8 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   if (!u) return fail(FACES_EINVAL, "null field");
   if (trials < 1) trials = 3;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (!(compute && !(c->flags & (FACES_GATHER | FACES_ROWS | FACES_V6)) && tile_kernel_supported(c->n))) return 0;
+  if (!(compute && !(c->flags & (FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F)) && tile_kernel_supported(c->n)))
+    return 0;
   // candidates: elements per tile (default, half, double), units of one
   // chunk or half a column (order 2 + 16*u), resident blocks per SM
   const int k0 = c->tplan.chunk;

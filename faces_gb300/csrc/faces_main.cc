@@ -18,6 +18,7 @@
 //   --gather          force the generic one-thread-per-point kernel
 //   --rows            use the register row kernel instead of the tile kernel
 //   --v6              v-6 strategy: six face messages per rank, sweeps z, y, x
+//   --v6f             the same in the fused form (four launches per share)
 //   --general         periodic fields: the general tile step
 //   --init=ref|int    initial state: gpu/main.cc:18 formula (default) or
 //                     integer values from --seed=S
@@ -77,6 +78,7 @@ int main(int argc, char *argv[])
     else if (s == "--gather") flags |= FACES_GATHER;
     else if (s == "--rows") flags |= FACES_ROWS;
     else if (s == "--v6") flags |= FACES_V6;
+    else if (s == "--v6f") flags |= FACES_V6F;
     else if (s == "--general") flags |= FACES_GENERAL;
     else if (s == "--json") json = true;
     else if (s == "--autotune") autotune = true;

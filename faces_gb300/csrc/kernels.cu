@@ -31,6 +31,7 @@
 #include "geom.cuh"
 #include "kernels.cuh"
 #include "rows_setup.cuh"
+#include "v6_steps.cuh"
 
 namespace faces {
 
@@ -688,126 +689,44 @@ cudaError_t launch_init_int(const FieldDesc &f, unsigned long long seed, cudaStr
 }
 
 // ---------------------------------------------------------------------------
-// v-6 (gpu/v-6-messages-basic/Faces.cc:65-173): six face messages per rank
-// and three dimension sweeps, z then y then x.  Face d of a rank holds the
-// n*n*m_a*m_b points of its low (i_d = 0, j_d = 0) or high (i_d = n-1,
-// j_d = m_d-1) plane, a < b the other two dimensions, point (ia, ib, ja, jb)
-// at ia + n*ib + n^2*ja + n^2*m_a*jb (the layout of zfs(ix,iy,jx,jy),
-// yfs(ix,iz,jx,jz), xfs(iy,iz,jy,jz)).  Per rank the buffer holds the x, y, z
-// faces, low then high.
+// v-6 (gpu/v-6-messages-basic/Faces.cc:65-173) and its fused form (v6_steps.cuh)
 // ---------------------------------------------------------------------------
 
-// Dimension d's sweep: a and b are the other two axes (a < b); sp* and se*
-// are the point and element strides of each axis, set on the host so that the
-// kernels index no array by a run-time axis (that would put it in local
-// memory).
-struct V6Geom {
-  int d, n, ma, mb, md;
-  long F, per_rank, off;  // face doubles, doubles per rank, offset of dimension d
-  long spa, spb, spd, sea, seb, sed;
-};
-
-V6Geom v6_geom(const FieldDesc &f, int d)
-{
-  V6Geom g;
-  g.d = d;
-  g.n = f.n;
-  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
-  const long n = f.n, nn = n * n;
-  const long sp[3] = {1, n, nn}, se[3] = {nn * n, f.sjy, f.sjz};
-  g.ma = f.m[a];
-  g.mb = f.m[b];
-  g.md = f.m[d];
-  g.spa = sp[a];
-  g.spb = sp[b];
-  g.spd = sp[d];
-  g.sea = se[a];
-  g.seb = se[b];
-  g.sed = se[d];
-  const long Fd[3] = {nn * f.m[1] * f.m[2], nn * f.m[0] * f.m[2], nn * f.m[0] * f.m[1]};
-  g.F = Fd[d];
-  g.per_rank = 2 * (Fd[0] + Fd[1] + Fd[2]);
-  g.off = 2 * (d > 0 ? Fd[0] : 0) + 2 * (d > 1 ? Fd[1] : 0);
-  return g;
-}
-
 long v6_message_doubles(const FieldDesc &f) { return v6_geom(f, 0).per_rank * f.nranks; }
-
-// face point idx of a dimension-d face: (ia, ib) fastest, then ja, then jb
-struct V6Point {
-  int ia, ib, ja, jb;
-  long off;  // ia*spa + ib*spb + ja*sea + jb*seb
-};
-
-template <typename I>
-__device__ __forceinline__ V6Point v6_point(const V6Geom &g, I idx)
-{
-  const I n = (I)g.n, nn = n * n, pa = nn * (I)g.ma;
-  V6Point p;
-  const I jb = idx / pa;
-  I q = idx - jb * pa;
-  const I ja = q / nn;
-  q -= ja * nn;
-  const I ib = q / n;
-  p.ia = (int)(q - ib * n);
-  p.ib = (int)ib;
-  p.ja = (int)ja;
-  p.jb = (int)jb;
-  p.off = p.ia * g.spa + p.ib * g.spb + p.ja * g.sea + p.jb * g.seb;
-  return p;
-}
 
 // every rank's two faces of dimension d, after the earlier sweeps
 template <typename I>
 __global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
 {
   const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
-  const I F2 = 2 * (I)g.F;
-  if (t >= (I)f.nranks * F2) return;
-  const I r = t / F2;
-  const I rem = t - r * F2;
-  const int side = rem >= (I)g.F;
-  const I idx = rem - (side ? (I)g.F : 0);
-  const V6Point p = v6_point(g, idx);
-  const long hi_off = side ? (long)(g.n - 1) * g.spd + (long)(g.md - 1) * g.sed : 0;
-  msg[(long)r * g.per_rank + g.off + (side ? g.F : 0) + (long)idx] = f.u[(long)r * f.R + p.off + hi_off];
+  if (t >= (I)f.nranks * 2 * (I)g.F) return;
+  v6_pack_item<I>(f, g, msg, t);
 }
 
-// low face += the lower neighbour's high face, element pairs along d, high
-// face += the upper neighbour's low face; compute = 0: element pairs only
-// where the point is on the subdomain boundary in another dimension
 template <typename I>
 __global__ void v6_update_kernel(FieldDesc f, V6Geom g, const double *msg, int compute)
 {
   const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
   if (t >= (I)f.nranks * (I)g.F) return;
-  const I r = t / (I)g.F;
-  const I idx = t - r * (I)g.F;
-  const int n = g.n, d = g.d;
-  const V6Point pt = v6_point(g, idx);
-  const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
-  const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
-  const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
-  const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
-  double *ur = f.u + (long)r * f.R + pt.off;
-  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
-  if (lo >= 0) {
-    double *p = ur;
-    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + (long)idx];
-  }
-  if (compute || on_a || on_b) {
-    double *p = ur + top;
-    for (int jd = 0; jd + 1 < g.md; jd++, p += g.sed) {
-      double *q = p + g.sed - top;
-      const double v = *p + *q;
-      *p = v;
-      *q = v;
-    }
-  }
-  if (hi >= 0) {
-    double *p = ur + top + (long)(g.md - 1) * g.sed;
-    *p = *p + msg[(long)hi * g.per_rank + g.off + (long)idx];
-  }
+  v6_update_item<I>(f, g, msg, compute, t);
+}
+
+// fused form, launch A
+template <typename I>
+__global__ void v6_early_kernel(FieldDesc f, V6Geoms gs, double *msg)
+{
+  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
+  if (t >= (I)f.nranks * (I)gs.g[0].per_rank) return;
+  v6_early_item<I>(f, gs, msg, t);
+}
+
+// fused form, launches B (d = 2) and C (d = 1)
+template <typename I>
+__global__ void v6_update_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg, int compute)
+{
+  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
+  if (t >= (I)f.nranks * (I)gs.g[d].F) return;
+  v6_update_pack_item<I>(f, gs, d, msg, compute, t);
 }
 
 cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
@@ -823,6 +742,31 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
       v6_pack_kernel<unsigned long><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
       v6_update_kernel<unsigned long><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
     }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
+{
+  const V6Geoms gs = v6_geoms(f);
+  const long na = (long)f.nranks * gs.g[0].per_rank;
+  // 32-bit index math while every thread index (and the next block's) fits
+  if (na + 256 < (1L << 31)) {
+    v6_early_kernel<unsigned><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(f, gs, msg);
+    for (int d = 2; d >= 1; d--) {
+      const long nu = (long)f.nranks * gs.g[d].F;
+      v6_update_pack_kernel<unsigned><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, gs, d, msg, compute);
+    }
+    const long nx = (long)f.nranks * gs.g[0].F;
+    v6_update_kernel<unsigned><<<(unsigned)((nx + 255) / 256), 256, 0, s>>>(f, gs.g[0], msg, compute);
+  } else {
+    v6_early_kernel<unsigned long><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(f, gs, msg);
+    for (int d = 2; d >= 1; d--) {
+      const long nu = (long)f.nranks * gs.g[d].F;
+      v6_update_pack_kernel<unsigned long><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, gs, d, msg, compute);
+    }
+    const long nx = (long)f.nranks * gs.g[0].F;
+    v6_update_kernel<unsigned long><<<(unsigned)((nx + 255) / 256), 256, 0, s>>>(f, gs.g[0], msg, compute);
   }
   return cudaGetLastError();
 }

@@ -20,6 +20,8 @@ cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 // (v6_message_doubles of them), sweeps z, y, x; six launches
 long v6_message_doubles(const FieldDesc &f);
 cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s);
+// its fused form (FACES_V6F; v6_steps.cuh): four launches, same messages and sums
+cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaStream_t s);
 
 // shared-memory tile step (tiles.cu): chunk (plan.chunk) at most tile_kinst_max(n)
 bool tile_kernel_supported(int n);

@@ -1,0 +1,250 @@
+// v6_steps.cuh -- the v-6 strategy's geometry and the bodies of its kernels
+// (host- and device-callable, so that tests/native/ptile_emu.cu replays them
+// on the CPU).
+//
+// v-6 (gpu/v-6-messages-basic/Faces.cc:65-173): six face messages per rank
+// and three dimension sweeps, z then y then x.  Face d of a rank holds the
+// n*n*m_a*m_b points of its low (i_d = 0, j_d = 0) or high (i_d = n-1,
+// j_d = m_d-1) plane, a < b the other two dimensions, point (ia, ib, ja, jb)
+// at ia + n*ib + n^2*ja + n^2*m_a*jb (the layout of zfs(ix,iy,jx,jy),
+// yfs(ix,iz,jx,jz), xfs(iy,iz,jy,jz)).  Per rank the buffer holds the x, y, z
+// faces, low then high.
+//
+// The fused form (v-6 overlap-fusable, gpu/v-6-messages-overlap-fusable/
+// Faces.cc:65-352, there to overlap the MPI transfers with the sweeps): a
+// sweep's thread owns one column along d and finishes every point of it, so
+// it can pack the next sweeps' messages for those points as soon as its own
+// update is done, and points that no later sweep changes can be packed before
+// the first one.  Four launches per share instead of six:
+//   A  every z face; the y-face points with iz interior; the x-face points
+//      with iy and iz interior (no sweep before theirs changes them);
+//   B  the z sweep; a thread whose column is on a y face packs its points
+//      (iz on a seam), one on an x face with iy interior packs its points;
+//   C  the y sweep; a thread whose column is on an x face packs its points
+//      (iy on a seam);
+//   D  the x sweep.
+// Every message point is packed exactly once, after the last sweep before
+// its own changed it, so the messages and the sums are those of the basic
+// form bit for bit.
+#pragma once
+
+#include "geom.cuh"
+#include "rows_setup.cuh"
+
+namespace faces {
+
+// Dimension d's sweep: a and b are the other two axes (a < b); sp* and se*
+// are the point and element strides of each axis, set on the host so that the
+// kernels index no array by a run-time axis (that would put it in local
+// memory).
+struct V6Geom {
+  int d, n, ma, mb, md;
+  long F, per_rank, off;  // face doubles, doubles per rank, offset of dimension d
+  long spa, spb, spd, sea, seb, sed;
+};
+
+inline V6Geom v6_geom(const FieldDesc &f, int d)
+{
+  V6Geom g;
+  g.d = d;
+  g.n = f.n;
+  const int a = d == 0 ? 1 : 0, b = d == 2 ? 1 : 2;
+  const long n = f.n, nn = n * n;
+  const long sp[3] = {1, n, nn}, se[3] = {nn * n, f.sjy, f.sjz};
+  g.ma = f.m[a];
+  g.mb = f.m[b];
+  g.md = f.m[d];
+  g.spa = sp[a];
+  g.spb = sp[b];
+  g.spd = sp[d];
+  g.sea = se[a];
+  g.seb = se[b];
+  g.sed = se[d];
+  const long Fd[3] = {nn * f.m[1] * f.m[2], nn * f.m[0] * f.m[2], nn * f.m[0] * f.m[1]};
+  g.F = Fd[d];
+  g.per_rank = 2 * (Fd[0] + Fd[1] + Fd[2]);
+  g.off = 2 * (d > 0 ? Fd[0] : 0) + 2 * (d > 1 ? Fd[1] : 0);
+  return g;
+}
+
+// the three sweeps' geometries (index = d)
+struct V6Geoms {
+  V6Geom g[3];
+};
+
+inline V6Geoms v6_geoms(const FieldDesc &f)
+{
+  V6Geoms s;
+  for (int d = 0; d < 3; d++) s.g[d] = v6_geom(f, d);
+  return s;
+}
+
+// face point idx of a dimension-d face: (ia, ib) fastest, then ja, then jb
+struct V6Point {
+  int ia, ib, ja, jb;
+  long off;  // ia*spa + ib*spb + ja*sea + jb*seb
+};
+
+template <typename I>
+FACES_HD V6Point v6_point(const V6Geom &g, I idx)
+{
+  const I n = (I)g.n, nn = n * n, pa = nn * (I)g.ma;
+  V6Point p;
+  const I jb = idx / pa;
+  I q = idx - jb * pa;
+  const I ja = q / nn;
+  q -= ja * nn;
+  const I ib = q / n;
+  p.ia = (int)(q - ib * n);
+  p.ib = (int)ib;
+  p.ja = (int)ja;
+  p.jb = (int)jb;
+  p.off = p.ia * g.spa + p.ib * g.spb + p.ja * g.sea + p.jb * g.seb;
+  return p;
+}
+
+// the position of point (ia, ib, ja, jb) in a dimension-g.d face
+FACES_HD long v6_face_index(const V6Geom &g, int ia, int ib, int ja, int jb)
+{
+  const long n = g.n;
+  return ia + n * ib + n * n * ja + n * n * g.ma * jb;
+}
+
+// the doubles of point (ia, ib, ja, jb) on side `side` of a dimension-g.d
+// face, from the rank's field ur (rank r's base)
+FACES_HD long v6_face_source(const V6Geom &g, const V6Point &p, int side)
+{
+  return p.off + (side ? (long)(g.n - 1) * g.spd + (long)(g.md - 1) * g.sed : 0);
+}
+
+// basic pack: thread t of nranks*2F -> one point of one side of every rank's
+// dimension-g.d faces
+template <typename I>
+FACES_HD void v6_pack_item(const FieldDesc &f, const V6Geom &g, double *msg, I t)
+{
+  const I F2 = 2 * (I)g.F;
+  const I r = t / F2;
+  const I rem = t - r * F2;
+  const int side = rem >= (I)g.F;
+  const I idx = rem - (side ? (I)g.F : 0);
+  const V6Point p = v6_point(g, idx);
+  msg[(long)r * g.per_rank + g.off + (side ? g.F : 0) + (long)idx] = f.u[(long)r * f.R + v6_face_source(g, p, side)];
+}
+
+// fused launch A: thread t of nranks*per_rank -> message position t (rank,
+// then x, y, z faces, low then high); packs the points no sweep before
+// theirs changes: z faces whole, y faces with iz interior, x faces with iy
+// and iz interior
+template <typename I>
+FACES_HD void v6_early_item(const FieldDesc &f, const V6Geoms &gs, double *msg, I t)
+{
+  const long pr = gs.g[0].per_rank;
+  const I r = t / (I)pr;
+  long rem = (long)(t - r * (I)pr);
+  int d = 0;
+  while (d < 2 && rem >= 2 * gs.g[d].F) {
+    rem -= 2 * gs.g[d].F;
+    d++;
+  }
+  const V6Geom &g = gs.g[d];
+  const int side = rem >= g.F;
+  const long idx = rem - (side ? g.F : 0);
+  const V6Point p = v6_point(g, idx);
+  const int n = g.n;
+  // dimension 1: b is z; dimension 0: a is y, b is z
+  if (d == 1 && (p.ib == 0 || p.ib == n - 1)) return;
+  if (d == 0 && (p.ia == 0 || p.ia == n - 1 || p.ib == 0 || p.ib == n - 1)) return;
+  msg[(long)r * pr + g.off + (side ? g.F : 0) + idx] = f.u[(long)r * f.R + v6_face_source(g, p, side)];
+}
+
+// One sweep (dimension g.d) over the column of face point idx of rank r: low
+// face += the lower neighbour's high face, element pairs along d, high face
+// += the upper neighbour's low face; compute = 0: element pairs only where
+// the point is on the subdomain boundary in another dimension.
+FACES_HD void v6_sweep_column(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, long r, long idx,
+                              const V6Point &pt)
+{
+  const int n = g.n, d = g.d;
+  const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
+  const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
+  const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
+  const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
+  double *ur = f.u + r * f.R + pt.off;
+  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
+  if (lo >= 0) {
+    double *p = ur;
+    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + idx];
+  }
+  if (compute || on_a || on_b) {
+    double *p = ur + top;
+    for (int jd = 0; jd + 1 < g.md; jd++, p += g.sed) {
+      double *q = p + g.sed - top;
+      const double v = *p + *q;
+      *p = v;
+      *q = v;
+    }
+  }
+  if (hi >= 0) {
+    double *p = ur + top + (long)(g.md - 1) * g.sed;
+    *p = *p + msg[(long)hi * g.per_rank + g.off + idx];
+  }
+}
+
+// basic update: thread t of nranks*F -> the column of one face point
+template <typename I>
+FACES_HD void v6_update_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
+{
+  const I r = t / (I)g.F;
+  const I idx = t - r * (I)g.F;
+  v6_sweep_column(f, g, msg, compute, (long)r, (long)idx, v6_point(g, idx));
+}
+
+// fused launches B (d = 2) and C (d = 1): the column's sweep, then the
+// messages of the later sweeps for the column's points (its seam points
+// along d: i_d in {0, n-1}, every j_d).  The sweep reads dimension d's
+// faces and the packs write the other dimensions': disjoint parts of msg.
+template <typename I>
+FACES_HD void v6_update_pack_item(const FieldDesc &f, const V6Geoms &gs, int d, double *msg, int compute, I t)
+{
+  const V6Geom &g = gs.g[d];
+  const I r = t / (I)g.F;
+  const I idx = t - r * (I)g.F;
+  const V6Point pt = v6_point(g, idx);
+  v6_sweep_column(f, g, msg, compute, (long)r, (long)idx, pt);
+  const int n = g.n;
+  const double *ur = f.u + (long)r * f.R;
+  const long pr = g.per_rank;
+  auto pack = [&](const V6Geom &h, int side, int ia, int ib, int ja, int jb, long src) {
+    msg[(long)r * pr + h.off + (side ? h.F : 0) + v6_face_index(h, ia, ib, ja, jb)] = ur[src];
+  };
+  const int nz = n - 1;
+  if (d == 2) {
+    // the thread's column: (ix, iy, jx, jy) = (ia, ib, ja, jb), along z
+    const int ix = pt.ia, iy = pt.ib, jx = pt.ja, jy = pt.jb;
+    const V6Geom &gy = gs.g[1], &gx = gs.g[0];
+    const int yside = (iy == 0 && jy == 0) ? 0 : (iy == nz && jy == f.m[1] - 1) ? 1 : -1;
+    const int xside = (ix == 0 && jx == 0) ? 0 : (ix == nz && jx == f.m[0] - 1) ? 1 : -1;
+    const bool x_interior_y = iy >= 1 && iy <= n - 2;
+    if (yside < 0 && (xside < 0 || !x_interior_y)) return;
+    for (int jz = 0; jz < f.m[2]; jz++)
+      for (int k = 0; k < 2; k++) {
+        const int iz = k ? nz : 0;
+        const long src = pt.off + (long)iz * g.spd + (long)jz * g.sed;
+        if (yside >= 0) pack(gy, yside, ix, iz, jx, jz, src);
+        if (xside >= 0 && x_interior_y) pack(gx, xside, iy, iz, jy, jz, src);
+      }
+  } else if (d == 1) {
+    // the thread's column: (ix, iz, jx, jz) = (ia, ib, ja, jb), along y
+    const int ix = pt.ia, iz = pt.ib, jx = pt.ja, jz = pt.jb;
+    const V6Geom &gx = gs.g[0];
+    const int xside = (ix == 0 && jx == 0) ? 0 : (ix == nz && jx == f.m[0] - 1) ? 1 : -1;
+    if (xside < 0) return;
+    for (int jy = 0; jy < f.m[1]; jy++)
+      for (int k = 0; k < 2; k++) {
+        const int iy = k ? nz : 0;
+        pack(gx, xside, iy, iz, jy, jz, pt.off + (long)iy * g.spd + (long)jy * g.sed);
+      }
+  }
+}
+
+}  // namespace faces

@@ -62,6 +62,14 @@ extern "C" {
                                1e-15 check otherwise).  compute = 0 sums only
                                subdomain-boundary points (the reference's v-6
                                ignores compute). */
+#define FACES_V6F 0x40u     /* v-6 in the fused form of gpu/v-6-messages-
+                               overlap-fusable/Faces.cc:65-352: each sweep's
+                               threads pack the later sweeps' messages for the
+                               points they finish, the points no sweep changes
+                               are packed up front; four launches per share
+                               instead of six, the same messages and sums as
+                               FACES_V6 bit for bit.  Not with FACES_V6 or
+                               FACES_MESSAGES. */
 
 typedef struct faces_ctx faces_ctx;
 

@@ -445,3 +445,87 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
   }
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// v-6, basic and fused (v6_steps.cuh): every launch's thread bodies run for
+// every thread index on the host, once in order and once in reverse order on
+// a copy (threads of one launch touch disjoint cells, so the two must agree
+// bit for bit); the message buffer starts each share as NaN between guard
+// cells, so a message read before it is packed poisons the result.
+// ---------------------------------------------------------------------------
+
+#include "v6_steps.cuh"
+
+namespace {
+
+template <class F>
+void launch_both_orders(long nthreads, double *u, long total, double *msg, long mtotal, F body, Err &e)
+{
+  std::vector<double> u2(u, u + total), m2(msg, msg + mtotal);
+  for (long t = 0; t < nthreads; t++) body(u, msg, t);
+  for (long t = nthreads - 1; t >= 0; t--) body(u2.data(), m2.data(), t);
+  if (std::memcmp(u2.data(), u, sizeof(double) * total) || std::memcmp(m2.data(), msg, sizeof(double) * mtotal))
+    e.set("a launch's result depends on the order of its threads", -1);
+}
+
+}  // namespace
+
+extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int fused, int compute,
+                          double *u, int nsteps, char *err, int errlen)
+{
+  Err e;
+  FieldDesc f{};
+  f.n = n;
+  f.m[0] = mx; f.m[1] = my; f.m[2] = mz;
+  f.L[0] = lx; f.L[1] = ly; f.L[2] = lz;
+  f.periodic = periodic;
+  f.mode = kDirect;
+  f.nranks = lx * ly * lz;
+  f.sjy = (long)n * n * n * mx;
+  f.sjz = jz_stride(n, mx, my);
+  f.R = f.sjz * mz;
+  const long total = f.R * f.nranks;
+  std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
+  f.nbr = nbr.data();
+  const V6Geoms gs = v6_geoms(f);
+  const long mtotal = gs.g[0].per_rank * f.nranks;
+  std::vector<double> field(total + 2 * kGuard, kSentinel), msg(mtotal + 2 * kGuard, kSentinel);
+  double *fu = field.data() + kGuard, *fm = msg.data() + kGuard;
+  std::memcpy(fu, u, sizeof(double) * total);
+  for (int step = 0; step < nsteps && e.ok; step++) {
+    std::fill(msg.begin() + kGuard, msg.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
+    auto with = [&](double *uu) {
+      FieldDesc g = f;
+      g.u = uu;
+      return g;
+    };
+    if (!fused) {
+      for (int d = 2; d >= 0 && e.ok; d--) {
+        const V6Geom &g = gs.g[d];
+        launch_both_orders(f.nranks * 2 * g.F, fu, total, fm, mtotal,
+                           [&](double *uu, double *mm, long t) { v6_pack_item<long>(with(uu), g, mm, t); }, e);
+        launch_both_orders(f.nranks * g.F, fu, total, fm, mtotal,
+                           [&](double *uu, double *mm, long t) { v6_update_item<long>(with(uu), g, mm, compute, t); }, e);
+      }
+    } else {
+      launch_both_orders(mtotal, fu, total, fm, mtotal,
+                         [&](double *uu, double *mm, long t) { v6_early_item<long>(with(uu), gs, mm, t); }, e);
+      for (int d = 2; d >= 1 && e.ok; d--)
+        launch_both_orders(f.nranks * gs.g[d].F, fu, total, fm, mtotal,
+                           [&](double *uu, double *mm, long t) {
+                             v6_update_pack_item<long>(with(uu), gs, d, mm, compute, t);
+                           },
+                           e);
+      launch_both_orders(f.nranks * gs.g[0].F, fu, total, fm, mtotal,
+                         [&](double *uu, double *mm, long t) { v6_update_item<long>(with(uu), gs.g[0], mm, compute, t); },
+                         e);
+    }
+    if (!guards_intact(field, total) || !guards_intact(msg, mtotal)) e.set("guard cells changed", -1);
+  }
+  std::memcpy(u, fu, sizeof(double) * total);
+  if (!e.ok) {
+    snprintf(err, errlen, "%s", e.msg.c_str());
+    return -1;
+  }
+  return 0;
+}

@@ -221,3 +221,38 @@ def test_warp_form_equals_alone(oracle, faces_lib, warp, half):
     b.close()
     for f, _ in fields:
         f.close()
+
+
+def test_v6_members_keep_their_order(faces_lib):
+    """v-6 fields sum in the order z, y, x; in a batch they run alone (one
+    faces_share each), so on the reference's non-integer init they still
+    give exactly their alone result, beside fields the batched kernel takes."""
+    F = faces_lib
+    specs = [((1, 1, 1, 3, 2, 4, 5), dict(periodic=True, v6=True)), ((2, 1, 1, 2, 3, 2, 6), dict(v6f=True)),
+             ((1, 1, 1, 4, 3, 2, 5), dict(periodic=True)), ((1, 2, 1, 3, 2, 2, 8), dict(periodic=True, v6f=True))]
+    def fields():
+        out = []
+        for sh, kw in specs:
+            f = F.Faces(*sh, **kw)
+            u = f.field()
+            f.init_ref(u)
+            out.append((f, u))
+        return out
+    exp = []
+    for f, u in fields():
+        f.share_n(u, 3)
+        torch.cuda.synchronize()
+        exp.append(u.cpu().numpy())
+        f.close()
+    got = fields()
+    b = F.Batch()
+    for f, u in got:
+        b.add(f, u)
+    b.commit()
+    assert b.info()["fused_fields"] == 1
+    b.share_n(3)
+    torch.cuda.synchronize()
+    for i, ((f, u), e) in enumerate(zip(got, exp)):
+        assert np.array_equal(u.cpu().numpy(), e), f"field {i}"
+        f.close()
+    b.close()

@@ -65,24 +65,25 @@ def test_c2_full_size_equals_oracle(oracle, faces_lib, mode):
     assert chk.passed and chk.maxrel == 0.0
 
 
-@pytest.mark.parametrize("mode", ["messages", "v6", "direct"])
+@pytest.mark.parametrize("mode", ["messages", "v6", "v6f", "direct"])
 def test_c3_full_size_equals_oracle(oracle, faces_lib, mode):
     """3x3x3 periodic virtual ranks of 16^3 elements, n=6, 3 shares."""
-    exp = expected(oracle, C3, 3, v6=mode == "v6")
-    out, chk = run(faces_lib, C3, 3, messages=mode == "messages", v6=mode == "v6")
+    exp = expected(oracle, C3, 3, v6=mode.startswith("v6"))
+    out, chk = run(faces_lib, C3, 3, messages=mode == "messages", v6=mode == "v6", v6f=mode == "v6f")
     assert np.array_equal(out, exp), f"{np.count_nonzero(out != exp)} points differ"
     assert chk.passed and chk.npass == 27
-    if mode == "v6":
+    if mode.startswith("v6"):
         assert np.array_equal(out, expected(oracle, C3, 3)), "v-6 differs from the group sums"
 
 
-@pytest.mark.parametrize("mode", ["direct", "messages", "v6"])
+@pytest.mark.parametrize("mode", ["direct", "messages", "v6", "v6f"])
 def test_reference_shape_open_equals_oracle(oracle, faces_lib, mode):
     """The reference's own argument set 1 1 1 15 14 13 12 (open, reference
     init, 2 shares): the same tree order as Mugs, so equal on any input."""
     shape = (1, 1, 1, 15, 14, 13, 12)
-    exp = expected(oracle, shape, 2, periodic=False, init="ref", v6=mode == "v6")
-    out, chk = run(faces_lib, shape, 2, periodic=False, init="ref", messages=mode == "messages", v6=mode == "v6")
+    exp = expected(oracle, shape, 2, periodic=False, init="ref", v6=mode.startswith("v6"))
+    out, chk = run(faces_lib, shape, 2, periodic=False, init="ref", messages=mode == "messages", v6=mode == "v6",
+                   v6f=mode == "v6f")
     assert np.array_equal(out, exp), f"{np.count_nonzero(out != exp)} points differ"
     assert chk.passed
 

@@ -163,16 +163,18 @@ def test_autotune_keeps_results(oracle, faces_lib, shape, periodic):
 
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
-def test_v6_bit_exact(oracle, faces_lib, shape, periodic):
-    """The v-6 strategy (six face messages, sweeps z, y, x) against the
-    oracle's v-6 restatement bit for bit, on both inits and with compute on
-    and off; on integer inputs also against the tree of the other modes."""
+@pytest.mark.parametrize("fused", [False, True], ids=["basic", "fused"])
+def test_v6_bit_exact(oracle, faces_lib, shape, periodic, fused):
+    """The v-6 strategy (six face messages, sweeps z, y, x; fused: four
+    launches, gpu/v-6-messages-overlap-fusable) against the oracle's v-6
+    restatement bit for bit, on both inits and with compute on and off; on
+    integer inputs also against the tree of the other modes."""
     O, F = oracle, faces_lib
     s = O.Shape(*shape, periodic=periodic)
     for init in ("int", "ref"):
         for compute in (True, False):
-            f = F.Faces(*shape, periodic=periodic, v6=True)
-            assert f.launches_per_share() == 6
+            f = F.Faces(*shape, periodic=periodic, v6=not fused, v6f=fused)
+            assert f.launches_per_share() == (4 if fused else 6)
             u = f.field()
             f.init_int(u, 5) if init == "int" else f.init_ref(u)
             f.share_n(u, 3, compute)
