@@ -81,11 +81,14 @@ void replan(faces_ctx &c)
   if (tile_kernel_supported(c.n)) {
     // the tile kernel is built for 1, 2, 4, ... tile_kinst_max(n) elements
     // per tile: a requested chunk rounds down to one of them
-    int k = c.chunk > 0 ? c.chunk : tile_default_chunk(c.n);
+    const bool general = (c.flags & FACES_GENERAL) || c.variant == 1;
+    const TileForm form = tile_form(f, general);
+    int k = c.chunk > 0 ? c.chunk : tile_default_chunk(c.n, form);
     int k2 = 1;
     while (k2 * 2 <= k && k2 * 2 <= tile_kinst_max(c.n)) k2 *= 2;
     k = k2;
-    while (k > 1 && tile_smem_bytes(c.n, k) > 110 * 1024) k /= 2;
+    // the form's shared memory at most 110 KB (two blocks per SM)
+    while (k > 1 && tile_form_smem_bytes(c.n, k, form) > 110 * 1024) k /= 2;
     c.tplan = make_row_plan(f, k, 0);
     // order 3 (warp tiles) applies to the periodic step only; elsewhere it
     // means the default
@@ -97,8 +100,7 @@ void replan(faces_ctx &c)
     // resident blocks per SM: shared memory (228 KB per SM, 1 KB reserved
     // per block) and 2048 threads of 256-thread blocks
     const bool periodic_step = (c.flags & FACES_PERIODIC) && !(c.flags & (FACES_MESSAGES | FACES_GENERAL));
-    const bool general = (c.flags & FACES_GENERAL) || c.variant == 1;
-    const int fit = tile_blocks_per_sm(c.n, k, tile_form(f, general));
+    const int fit = tile_blocks_per_sm(c.n, k, form);
     const int per_sm = c.tpb > 0 ? (c.tpb < fit ? c.tpb : fit) : fit;
     c.tgrid = (long)c.sms * (per_sm < 1 ? 1 : per_sm);
     if (periodic_step && c.order >= 0 && c.order % 16 == 3) {

@@ -32,6 +32,10 @@ size_t tile_smem_bytes(int n, int chunk);
 enum TileForm : int { kGeneralForm = 0, kPeriodicForm = 1, kExchangeForm = 2 };
 TileForm tile_form(const FieldDesc &f, bool general);
 int tile_blocks_per_sm(int n, int chunk, TileForm form);
+// shared memory of one block of a tile form
+size_t tile_form_smem_bytes(int n, int chunk, TileForm form);
+// the default tile length of a form
+int tile_default_chunk(int n, TileForm form);
 // the warp-tile form of the periodic step (periodic direct-mode fields; plan
 // chunk at most tile_kwarp(n)); grid in blocks of 4 warps
 size_t wtile_smem_bytes(int n);

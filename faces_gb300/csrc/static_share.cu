@@ -204,16 +204,17 @@ extern "C" int faces_share_static(double *u, int lx, int ly, int lz, int mx, int
     if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
         (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
       return fail(FACES_ECUDA, "faces_share_static: device query: %s", cudaGetErrorString(e));
-    // the default plan of faces_share for a message-mode field: tiles of
-    // tile_default_chunk(n) elements (halved while three stages exceed
-    // 110 KB), units of half a column, the resident blocks per SM that
-    // shared memory and the launch bounds of the field's tile kernel allow
-    int k = tile_default_chunk(n);
-    while (k > 1 && tile_smem_bytes(n, k) > 110 * 1024) k /= 2;
+    // the default plan of faces_share for a message-mode field: the field's
+    // tile form, its default tile length (halved while the form's shared
+    // memory exceeds 110 KB), units of half a column, the resident blocks per
+    // SM that shared memory and the form's launch bounds allow
+    const TileForm form = tile_form(f, false);
+    int k = tile_default_chunk(n, form);
+    while (k > 1 && tile_form_smem_bytes(n, k, form) > 110 * 1024) k /= 2;
     RowPlan p = make_row_plan(f, k, 0);
     p.order = 2;
     p.unit_chunks = (p.nchunks + 1) / 2;
-    e = launch_tiles(f, p, (long)sms * tile_blocks_per_sm(n, k, tile_form(f, false)), s);
+    e = launch_tiles(f, p, (long)sms * tile_blocks_per_sm(n, k, form), s);
   } else {
     e = launch_gather(f, compute, s);
   }

@@ -57,6 +57,25 @@ def batch_warp_tile(n, stage=2688):
     return min(32, (w - 2 * n * n) // (n * n * row_stride(n)))
 
 
+def form_default_k(n, form):
+    """the default tile length of the periodic ("p") and message-mode ("x")
+    steps: for n >= 10 the longest power of 2 whose three stages and tile
+    records stay within 110 KB (PMeta 80 B + int4 per stage; XMeta 240 B per
+    record, one more record than stages)"""
+    if n < 10:
+        return tile_kmax(n)
+    rec = 3 * 96 if form == "p" else 4 * 240
+    k = 1
+    while k * 2 <= max(tile_kmax(n), 8) and 8 * 3 * (2 * k * n * n * row_stride(n) + 2 * n * n) + rec <= 110 * 1024:
+        k *= 2
+    return k
+
+
+def test_form_default_lengths():
+    assert [form_default_k(n, "p") for n in (10, 11, 12)] == [4, 2, 2]
+    assert [form_default_k(n, "x") for n in (10, 11, 12)] == [4, 2, 2]
+
+
 def tile_kwarp(n):
     """the warp form's tile length (about 6 KB of stage)"""
     v = 6144 // (n * n * row_stride(n) * 8)
@@ -66,7 +85,7 @@ def tile_kwarp(n):
 def cases():
     out = []
     for n in range(2, 13):
-        ks = sorted({1, 2, tile_kmax(n)} | ({batch_tile(n)} if n <= 10 else set()))
+        ks = sorted({1, 2, tile_kmax(n), form_default_k(n, "p")} | ({batch_tile(n)} if n <= 10 else set()))
         for K in ks:
             out.append((n, K, 256))
         for K in sorted({tile_kmax(n), tile_kwarp(n)} | ({batch_warp_tile(n)} if n <= 5 else set())):
@@ -121,7 +140,7 @@ def xemu():
 def xcases():
     out = []
     for n in range(2, 13):
-        for K in sorted({1, 2, tile_kmax(n)}):
+        for K in sorted({1, 2, tile_kmax(n), form_default_k(n, "x")}):
             out.append((n, K, 256))
         out.append((n, tile_kmax(n), 32))
     return out
