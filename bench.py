@@ -67,6 +67,8 @@ RESEED_EVERY = 100
 def kernel_name(t: dict) -> str:
     """The step's kernel for n = 8 on this field from faces_get_tuning."""
     k = 1 << max(0, (t["chunk"] - 1).bit_length())
+    if t["kernel"] == 3:
+        return "faces::seam_kernel<8>"
     if t["kernel"] == 2:
         return "faces::rows_kernel<8>"
     if t["kernel"] == 1:
@@ -319,7 +321,7 @@ def run_faces(args) -> dict | None:
             f.run_host_many(ins, outs, E2E_SHARES, True, stream)
         el = max_over_ranks(time.perf_counter() - t0)
         # the downloaded results are the closed form of 100 shares
-        probe = torch.from_numpy(outs[-1]).to(dev)
+        probe = torch.from_numpy(outs[-1]).to(u.device)
         e2e_chk = f.check(probe, init="int", seed=SEED, nshares=E2E_SHARES)
         del probe
         f.run_host(hi[0], ho[0], E2E_SHARES, True, stream)  # warm-up

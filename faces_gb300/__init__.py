@@ -29,6 +29,7 @@ ROWS = 0x8
 GENERAL = 0x10
 V6 = 0x20
 V6F = 0x40
+SEAMS = 0x80
 
 _ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
 
@@ -210,19 +211,22 @@ class Faces:
                 (gpu/v-6-messages-basic/Faces.cc:65-173)
     v6f      -- v-6 in the fused form of gpu/v-6-messages-overlap-fusable/
                 Faces.cc: four launches per share, the same results as v6
+    seams    -- the seam kernel: one thread per shared point of each
+                element's lower seam planes, no shared memory (direct mode)
     """
 
     def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
                  periodic: bool = False, messages: bool = False, gather: bool = False, rows: bool = False,
-                 general: bool = False, v6: bool = False, v6f: bool = False):
+                 general: bool = False, v6: bool = False, v6f: bool = False, seams: bool = False):
         flags = ((PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
-                 | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0) | (V6F if v6f else 0))
+                 | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0) | (V6F if v6f else 0)
+                 | (SEAMS if seams else 0))
         h = ctypes.c_void_p()
         _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
         self._h = h
         self.shape = (lx, ly, lz, mx, my, mz, n)
         self.periodic, self.messages, self.gather, self.rows = periodic, messages, gather, rows
-        self.general, self.v6, self.v6f = general, v6, v6f
+        self.general, self.v6, self.v6f, self.seams = general, v6, v6f, seams
         s = (ctypes.c_long * 6)()
         rd, tot = ctypes.c_long(), ctypes.c_long()
         _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
@@ -323,7 +327,8 @@ class Faces:
     def set_tuning(self, chunk: int = 0, width: int = 0, order: int = -1) -> None:
         """Elements per x-chunk, width (row kernel: tiles per block; tile
         kernel: resident blocks per SM) and tile order (0 strided, 1
-        contiguous); 0 / -1 keep the defaults."""
+        contiguous; seam kernel: 0 chunked, 1 lean); 0 / -1 keep the
+        defaults (and the default kernel)."""
         _check(lib().faces_set_tuning(self._h, chunk, width, order))
 
     def autotune(self, u, compute: bool = True, trials: int = 3, stream=None) -> int:
@@ -363,7 +368,8 @@ class Batch:
         lx, ly, lz, mx, my, mz, n = faces.shape
         flags = ((PERIODIC if faces.periodic else 0) | (MESSAGES if faces.messages else 0)
                  | (GATHER if faces.gather else 0) | (ROWS if faces.rows else 0)
-                 | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0) | (V6F if faces.v6f else 0))
+                 | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0) | (V6F if faces.v6f else 0)
+                 | (SEAMS if faces.seams else 0))
         fid = ctypes.c_int()
         _check(lib().faces_batch_add(self._h, _ptr(u), lx, ly, lz, mx, my, mz, n, flags, ctypes.byref(fid)))
         self._fields.append(u)

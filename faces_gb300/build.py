@@ -33,7 +33,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contra
 
 # (source, object); the row kernel's instantiations are split over several
 # units so they compile in parallel
-UNITS = (["faces_api.cu", "kernels.cu", "tiles.cu", "static_share.cu", "batch.cu", "serve.cu"]
+UNITS = (["faces_api.cu", "kernels.cu", "tiles.cu", "seams.cu", "static_share.cu", "batch.cu", "serve.cu"]
          + [f"tiles_n{n}.cu" for n in range(2, 13)]
          + [f"batch_k{f}.cu" for f in ("00", "20", "10", "11", "12")])
 

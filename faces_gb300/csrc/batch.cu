@@ -166,7 +166,7 @@ namespace {
 bool batch_eligible(const faces_ctx *c)
 {
   // message strategies keep their own order of sums: one faces_share each
-  return batch_n_supported(c->n) && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F));
+  return batch_n_supported(c->n) && !(c->flags & (FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F | FACES_SEAMS));
 }
 
 void drop_graphs(faces_batch *b)

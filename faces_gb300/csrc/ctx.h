@@ -7,6 +7,7 @@
 
 #include "../../include/faces_gb300.h"
 #include "geom.cuh"
+#include "kernels.cuh"
 #include "rows_setup.cuh"
 
 struct faces_ctx {
@@ -36,9 +37,11 @@ struct faces_ctx {
   int sms = 0;       // multiprocessors of the device
   faces::RowPlan plan;   // row kernel
   faces::RowPlan tplan;  // tile kernel
+  faces::SeamPlan splan{};  // seam kernel
   long tgrid = 0;    // tile kernel CTAs
-  int variant = 0;   // set by faces_autotune: 0 the tile step (periodic or mixed),
-                     // 1 the general tile step, 2 the row kernel
+  int variant = 0;   // the kernel (default, or set by faces_autotune): 0 the tile step
+                     // (periodic or mixed), 1 the general tile step, 2 the row
+                     // kernel, 3 the seam kernel
 
   faces::FieldDesc desc(double *u) const
   {

@@ -74,10 +74,40 @@ int default_chunk(const faces_ctx &c)
   return (int)((c.m[0] + nch - 1) / nch);
 }
 
+// the seam kernel runs this share: forced, the default, or chosen by
+// autotune (variant 3)
+bool seam_step(const faces_ctx &c)
+{
+  return (c.variant == 3 || (c.flags & FACES_SEAMS)) && seam_kernel_supported(c.n) &&
+         !(c.flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F | FACES_GATHER));
+}
+
+// The default kernel: the seam kernel for direct-mode fields with n >= 12,
+// where it moves more than the tile step (95x94x93 n = 12: 4.00 ms per share
+// against 4.90 open, 4.34 periodic; 15x14x13 n = 12: 0.023 against 0.029)
+// and the tile step does not reach past n = 12; else the tile step.
+int default_variant(const faces_ctx &c)
+{
+  return c.n >= 12 && seam_kernel_supported(c.n) &&
+                 !(c.flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F | FACES_GATHER | FACES_ROWS | FACES_GENERAL))
+             ? 3
+             : 0;
+}
+
 void replan(faces_ctx &c)
 {
   const FieldDesc f = c.desc(nullptr);
   c.plan = make_row_plan(f, c.chunk > 0 ? c.chunk : default_chunk(c), c.tpb);
+  if (seam_step(c)) {
+    // resident blocks per SM from the kernel's occupancy (or the width asked for)
+    const int fit = seam_blocks_per_sm(c.n);
+    // order 1: the lean form, 0: the chunked form; by default the lean form
+    // where it gives the GPU four waves of threads (measured: 95x94x93 n = 12
+    // 4.00 ms lean, 4.82 chunked; 15x14x13 n = 12 0.031 lean, 0.023 chunked)
+    const long lean_threads = (long)c.nranks * c.m[0] * c.m[1] * c.m[2] * (c.n > 2 ? (c.n - 2) * (c.n - 2) : 1);
+    const bool lean = c.order == 1 || (c.order < 0 && lean_threads >= 4L * c.sms * 6 * 256);
+    c.splan = make_seam_plan(f, c.chunk, (long)c.sms * (c.tpb > 0 && c.tpb < fit ? c.tpb : fit), lean);
+  }
   if (tile_kernel_supported(c.n)) {
     // the tile kernel is built for 1, 2, 4, ... tile_kinst_max(n) elements
     // per tile: a requested chunk rounds down to one of them
@@ -140,8 +170,11 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   if (lx < 1 || ly < 1 || lz < 1) return fail(FACES_EINVAL, "rank grid %d x %d x %d must be positive", lx, ly, lz);
   if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
   if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
-  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL | FACES_V6 | FACES_V6F))
+  if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL | FACES_V6 | FACES_V6F |
+                FACES_SEAMS))
     return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
+  if ((flags & FACES_SEAMS) && (flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F)))
+    return fail(FACES_EINVAL, "FACES_SEAMS sums every copy in place: not with a message strategy");
   if (((flags & FACES_V6) != 0) + ((flags & FACES_V6F) != 0) + ((flags & FACES_MESSAGES) != 0) > 1)
     return fail(FACES_EINVAL, "FACES_V6, FACES_V6F and FACES_MESSAGES are message strategies: choose one");
   const long nranks = (long)lx * ly * lz;
@@ -185,6 +218,7 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
     faces_destroy(c);
     return cuda_fail(e, "faces_create: device query");
   }
+  c->variant = default_variant(*c);
   replan(*c);
   *out = c;
   return FACES_OK;
@@ -250,7 +284,7 @@ int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
   c->chunk = chunk > 0 ? chunk : 0;
   c->tpb = width > 0 ? width : 0;
   c->order = order;
-  c->variant = 0;
+  c->variant = default_variant(*c);
   replan(*c);
   return FACES_OK;
 }
@@ -258,20 +292,21 @@ int faces_set_tuning(faces_ctx *c, int chunk, int width, int order)
 int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order)
 {
   if (int rc = check_ctx(c)) return rc;
-  if (kernel) *kernel = c->variant;
-  if (order) *order = c->tplan.order;
-  if (chunk) *chunk = c->tplan.chunk;
-  if (unit_chunks) *unit_chunks = c->tplan.unit_chunks;
-  if (blocks) *blocks = (int)c->tgrid;
+  const bool seams = seam_step(*c);
+  if (kernel) *kernel = seams ? 3 : c->variant;
+  if (order) *order = seams ? c->splan.lean : c->tplan.order;
+  if (chunk) *chunk = seams ? c->splan.chunk : c->tplan.chunk;
+  if (unit_chunks) *unit_chunks = seams ? 1 : c->tplan.unit_chunks;
+  if (blocks) *blocks = (int)(seams ? c->splan.grid : c->tgrid);
   return FACES_OK;
 }
 
 int faces_launches_per_share(const faces_ctx *c, int compute)
 {
   if (int rc = check_ctx(c)) return rc;
-  (void)compute;
   if (c->flags & FACES_V6) return 6;
   if (c->flags & FACES_V6F) return 4;
+  if (compute && seam_step(*c) && c->splan.lean && c->splan.plane_items > 0) return 2;
   return (c->flags & FACES_MESSAGES) ? 2 : 1;
 }
 
@@ -288,6 +323,10 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   }
   if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   const bool fused = compute && !(c->flags & FACES_GATHER);
+  if (fused && seam_step(*c)) {
+    CUDA_TRY(launch_seams(f, c->splan, s), "seam kernel launch");
+    return FACES_OK;
+  }
   if (fused && !(c->flags & FACES_ROWS) && c->variant != 2 && tile_kernel_supported(c->n)) {
     const bool general = (c->flags & FACES_GENERAL) || c->variant == 1;
     if (c->tplan.order == 3 && !general) CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
@@ -322,7 +361,8 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   if (!u) return fail(FACES_EINVAL, "null field");
   if (trials < 1) trials = 3;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (!(compute && !(c->flags & (FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F)) && tile_kernel_supported(c->n)))
+  if (!(compute && !(c->flags & (FACES_GATHER | FACES_ROWS | FACES_V6 | FACES_V6F | FACES_SEAMS)) &&
+        tile_kernel_supported(c->n)))
     return 0;
   // candidates: elements per tile (default, half, double), units of one
   // chunk or half a column (order 2 + 16*u), resident blocks per SM
@@ -376,6 +416,21 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   c->tpb = 0;
   if (rc == FACES_OK && !periodic_step && !(c->flags & FACES_GENERAL)) trial(1);
   if (rc == FACES_OK && row_kernel_supported(c->n)) trial(2);
+  // the seam kernel (direct mode): the chunked form (order 0) at its
+  // default chunk and twice it, and the lean form (order 1)
+  if (!(c->flags & FACES_MESSAGES) && seam_kernel_supported(c->n)) {
+    const int e0 = seam_default_chunk(c->n);
+    c->order = 0;
+    for (int e : {e0, 2 * e0}) {
+      if (rc != FACES_OK) break;
+      c->chunk = e;
+      trial(3);
+    }
+    c->chunk = 0;
+    c->order = 1;
+    if (rc == FACES_OK) trial(3);
+    c->order = -1;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   c->chunk = bk;

@@ -77,6 +77,7 @@ int main(int argc, char *argv[])
     else if (s == "--messages") flags |= FACES_MESSAGES;
     else if (s == "--gather") flags |= FACES_GATHER;
     else if (s == "--rows") flags |= FACES_ROWS;
+    else if (s == "--seams") flags |= FACES_SEAMS;
     else if (s == "--v6") flags |= FACES_V6;
     else if (s == "--v6f") flags |= FACES_V6F;
     else if (s == "--general") flags |= FACES_GENERAL;

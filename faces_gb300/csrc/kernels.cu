@@ -31,6 +31,7 @@
 #include "geom.cuh"
 #include "kernels.cuh"
 #include "rows_setup.cuh"
+#include "seam_steps.cuh"
 #include "v6_steps.cuh"
 
 namespace faces {
@@ -182,99 +183,7 @@ __global__ void pack_kernel(FieldDesc f)
 // gather: one thread per owned shared point (any n, compute on or off)
 // ---------------------------------------------------------------------------
 
-// Rank-local point coordinate g in [0, m*(n-1)] along one axis: element E
-// holds g = E*(n-1)+i.  A point with g % (n-1) == 0 has a lower copy (E-1,
-// n-1) and an upper copy (E, 0); elements -1 and m belong to the neighbours.
-// Scalars (and loops unrolled over fixed bounds below), so that no array is
-// indexed at run time and nothing goes to local memory.
-struct Copies {
-  int cnt, e0, i0, e1, i1;
-};
-
-__device__ __forceinline__ Copies local_axis(int g, int n)
-{
-  const int nm1 = n - 1, E = g / nm1, i = g % nm1;
-  if (i) return Copies{1, E, i, E, i};
-  return Copies{2, E - 1, nm1, E, 0};
-}
-
-// One shared point: point g (global in rank r's subdomain) and its copies,
-// summed as a tree x, y, z and written to every local copy.  Points that are
-// not shared, or that another rank owns (direct mode), return at once.
-__device__ __forceinline__ void gather_point(const FieldDesc &f, int r, const int g[3], int compute)
-{
-  const int n = f.n, nm1 = n - 1;
-  // a point is shared only if it lies on an element boundary somewhere
-  if (g[0] % nm1 && g[1] % nm1 && g[2] % nm1) return;
-  bool onb = false, skip = false;
-  Copies c[3];
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const int Ga = f.m[a] * nm1;
-    onb |= (g[a] == 0 || g[a] == Ga);
-    // direct mode: the upper rank owns the points of the shared plane
-    if (f.mode == kDirect && g[a] == Ga && nbr_of(f, r, dir_index(a == 0, a == 1, a == 2)) >= 0) skip = true;
-    Copies x = local_axis(g[a], n);
-    // drop copies whose neighbour rank does not exist
-    auto exists = [&](int e) {
-      const int dv = e < 0 ? -1 : (e >= f.m[a] ? 1 : 0);
-      return dv == 0 || nbr_of(f, r, dir_index(a == 0 ? dv : 0, a == 1 ? dv : 0, a == 2 ? dv : 0)) >= 0;
-    };
-    const bool ok0 = exists(x.e0), ok1 = x.cnt == 2 && exists(x.e1);
-    if (!ok0) { x.e0 = x.e1; x.i0 = x.i1; }
-    x.cnt = (int)ok0 + (int)ok1;
-    c[a] = x;
-  }
-  if (skip) return;
-  if (c[0].cnt * c[1].cnt * c[2].cnt < 2) return;
-  if (!compute && !onb) return;
-  double v[2][2][2];
-  double *w[2][2][2];
-#pragma unroll
-  for (int bz = 0; bz < 2; bz++)
-#pragma unroll
-    for (int by = 0; by < 2; by++)
-#pragma unroll
-      for (int bx = 0; bx < 2; bx++) {
-        w[bz][by][bx] = nullptr;
-        v[bz][by][bx] = 0.0;
-        if (bz >= c[2].cnt || by >= c[1].cnt || bx >= c[0].cnt) continue;
-        const int e[3] = {bx ? c[0].e1 : c[0].e0, by ? c[1].e1 : c[1].e0, bz ? c[2].e1 : c[2].e0};
-        const int i[3] = {bx ? c[0].i1 : c[0].i0, by ? c[1].i1 : c[1].i0, bz ? c[2].i1 : c[2].i0};
-        int d[3], j[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-          d[a] = e[a] < 0 ? -1 : (e[a] >= f.m[a] ? 1 : 0);
-          j[a] = e[a] < 0 ? f.m[a] - 1 : (e[a] >= f.m[a] ? 0 : e[a]);
-        }
-        const int dir = dir_index(d[0], d[1], d[2]);
-        if (dir == 13 || f.mode == kDirect) {
-          const int q = (dir == 13) ? r : nbr_of(f, r, dir);
-          double *ptr = f.u + (long)q * f.R + elem_index(f, i[0], i[1], i[2], j[0], j[1], j[2]);
-          w[bz][by][bx] = ptr;
-          v[bz][by][bx] = *ptr;
-        } else {
-          const double *rb = recv_of(f, r, dir);
-          v[bz][by][bx] = rb[region_pos(f, d, i, j)];
-        }
-      }
-  double sy[2];
-#pragma unroll
-  for (int bz = 0; bz < 2; bz++) {
-    double sx[2];
-#pragma unroll
-    for (int by = 0; by < 2; by++) sx[by] = (c[0].cnt == 2) ? v[bz][by][0] + v[bz][by][1] : v[bz][by][0];
-    sy[bz] = (c[1].cnt == 2) ? sx[0] + sx[1] : sx[0];
-  }
-  const double s = (c[2].cnt == 2) ? sy[0] + sy[1] : sy[0];
-#pragma unroll
-  for (int bz = 0; bz < 2; bz++)
-#pragma unroll
-    for (int by = 0; by < 2; by++)
-#pragma unroll
-      for (int bx = 0; bx < 2; bx++)
-        if (w[bz][by][bx]) *w[bz][by][bx] = s;
-}
+// gather_point (seam_steps.cuh): one point, its copies, the tree sum
 
 __global__ void gather_kernel(FieldDesc f, int compute)
 {

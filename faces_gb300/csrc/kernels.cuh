@@ -16,6 +16,20 @@ cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s);
 cudaError_t launch_gather(const FieldDesc &f, int compute, cudaStream_t s);
 cudaError_t launch_rows(const FieldDesc &f, const RowPlan &p, cudaStream_t s);
 
+// seam step (seams.cu, seam_steps.cuh): direct mode, compute = true; the
+// chunked form (chunks of `chunk` elements along x, `grid` blocks) or the
+// lean form
+struct SeamPlan {
+  int chunk, nch;
+  long units, plane_items, grid;
+  int lean;  // the lean form: a thread per face slot (and the boundary planes' launch)
+};
+bool seam_kernel_supported(int n);
+int seam_default_chunk(int n);
+int seam_blocks_per_sm(int n);
+SeamPlan make_seam_plan(const FieldDesc &f, int chunk, long grid, int lean);
+cudaError_t launch_seams(const FieldDesc &f, const SeamPlan &p, cudaStream_t s);
+
 // v-6 strategy (FACES_V6): six face messages per rank in `msg`
 // (v6_message_doubles of them), sweeps z, y, x; six launches
 long v6_message_doubles(const FieldDesc &f);

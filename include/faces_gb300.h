@@ -70,6 +70,15 @@ extern "C" {
                                instead of six, the same messages and sums as
                                FACES_V6 bit for bit.  Not with FACES_V6 or
                                FACES_MESSAGES. */
+#define FACES_SEAMS 0x80u   /* use the seam kernel: one thread per shared
+                               point of each element's lower seam planes
+                               (the point-per-thread form of gpu/v-26-
+                               messages/Faces.cc:301-343), no shared memory;
+                               direct mode only (not with FACES_MESSAGES,
+                               FACES_V6 or FACES_V6F).  Without it the seam
+                               kernel is still the default for direct-mode
+                               fields with n >= 12 (FACES_ROWS and
+                               FACES_GENERAL keep theirs). */
 
 typedef struct faces_ctx faces_ctx;
 
@@ -149,13 +158,20 @@ int faces_run_host_many(faces_ctx *ctx, int njobs, const double *const *u_in, do
  * 1: each block takes a contiguous range of x-chunks, 2 + 16*u: blocks stride
  * over units of u consecutive x-chunks of a column, listed chunk group first,
  * u = 0 half a column; 3: periodic step only, one warp per tile instead of
- * one block, no block barriers). */
+ * one block, no block barriers).  With the seam kernel (FACES_SEAMS, and
+ * the default for direct-mode fields with n >= 12): elements per x-chunk of
+ * its chunked form, resident blocks per SM, and the form (order 0 chunked,
+ * 1 lean: one thread per face slot of every element, plus a launch for the
+ * open boundary planes; < 0: lean where the field gives four waves of
+ * threads).  Returns to the default kernel. */
 int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 
 /* Times the tile step on the field u over elements per tile (default, half,
  * double), units (half a column, one chunk, warp tiles) and resident blocks
- * per SM (default, 2), and the general tile step and the row kernel at their
- * defaults, `trials` shares each after one warm-up, and keeps the fastest
+ * per SM (default, 2), the general tile step and the row kernel at their
+ * defaults, and in direct mode the seam kernel (chunked at two chunk
+ * lengths; lean), `trials` shares each after one warm-up, and keeps the
+ * fastest
  * (faces_set_tuning's settings and the kernel; faces_set_tuning returns to
  * the tile step).  Every timed launch is a share of
  * u: returns how many it applied (>= 0; re-initialise u afterwards) or an
@@ -165,8 +181,9 @@ int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *str
 
 /* The tile step's current settings: elements per tile, x-chunks per unit
  * of work, blocks launched, the kernel (0 the tile step, 1 the general tile
- * step, 2 the row kernel) and the tile order (as faces_set_tuning; 3 warp
- * tiles).  Any pointer may be NULL. */
+ * step, 2 the row kernel, 3 the seam kernel) and the tile order (as
+ * faces_set_tuning; 3 warp tiles; seam kernel: 0 chunked, 1 lean).  Any
+ * pointer may be NULL. */
 int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order);
 
 /* Kernel launches one share enqueues with the current settings. */

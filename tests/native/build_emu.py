@@ -29,7 +29,7 @@ def build_ptile() -> str:
     csrc = os.path.join(ROOT, "faces_gb300", "csrc")
     deps = [src] + [os.path.join(csrc, f) for f in ("geom.cuh", "rows_setup.cuh", "tables.h", "tile_ops.cuh",
                                                      "tile_steps.cuh", "ptile_steps.cuh",
-                                                     "xtile_steps.cuh", "v6_steps.cuh")]
+                                                     "xtile_steps.cuh", "v6_steps.cuh", "seam_steps.cuh")]
     if os.path.exists(PTILE_OUT) and all(os.path.getmtime(d) <= os.path.getmtime(PTILE_OUT) for d in deps):
         return PTILE_OUT
     os.makedirs(os.path.dirname(PTILE_OUT), exist_ok=True)

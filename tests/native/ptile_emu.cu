@@ -529,3 +529,123 @@ extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n,
   }
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// The seam step (seam_steps.cuh): every slot of every chunk, then every item
+// of the open upper boundary planes, run one by one.  The kernel has no
+// barrier, so its threads may run in any order and at once: each point may be
+// read and written by one thread of a share at most (every touched address is
+// recorded with its thread), and every address must lie in the field.
+// ---------------------------------------------------------------------------
+
+#include "seam_steps.cuh"
+
+namespace {
+
+// the lean form: the lean kernel's items, then the boundary planes' (each
+// launch in order or in reverse); one thread per item
+template <int N, class T>
+void seam_lean_share(const FieldDesc &f, bool reverse, long &who, T touch, Err &e)
+{
+  const long items = (long)f.nranks * f.m[0] * f.m[1] * f.m[2] * seam_lean_slots(N);
+  const long planes = f.periodic ? 0 : (long)f.nranks * seam_plane_items(f);
+  for (long k = 0; k < items && e.ok; k++) {
+    const long g = reverse ? items - 1 - k : k;
+    who = g;
+    seam_lean_item<N>(f, g, touch);
+  }
+  for (long k = 0; k < planes && e.ok; k++) {
+    const long g = reverse ? planes - 1 - k : k;
+    who = items + g;
+    seam_plane_point(f, g, touch);
+  }
+}
+
+template <int N>
+void seam_share(const FieldDesc &f, int E, bool reverse, bool lean, Err &e)
+{
+  constexpr int S = seam_slots(N);
+  const long total = f.R * f.nranks;
+  const int nch = (f.m[0] + E - 1) / E;
+  const long units = (long)f.nranks * f.m[2] * f.m[1] * nch;
+  const long planes = f.periodic ? 0 : (long)f.nranks * seam_plane_items(f);
+  std::vector<long> owner(total, -1);
+  long who = 0;
+  auto touch = [&](const double *p) {
+    const long i = (long)(p - f.u);
+    if (i < 0 || i >= total) { e.set("an address outside the field", who); return; }
+    if (owner[i] >= 0 && owner[i] != who) { e.set("a point touched by two threads of one share", who); return; }
+    owner[i] = who;
+  };
+  if (lean) {
+    seam_lean_share<N>(f, reverse, who, touch, e);
+    return;
+  }
+  // the kernel's loop: thread t of a 256-thread block takes slots t, t+256,
+  // ... of each chunk; who = (chunk, thread)
+  constexpr int T = 256;
+  const long threads = units * T;
+  for (long k = 0; k < threads + planes && e.ok; k++) {
+    const long id = reverse ? threads + planes - 1 - k : k;
+    who = id;
+    if (id < threads) {
+      const long w = id / T;
+      const int t = (int)(id - w * T);
+      const SeamUnit un = seam_unit(f, E, nch, w);
+      const SeamChunk c = seam_chunk<N>(f, un.r, un.jy, un.jz, un.jx0, un.nk);
+      const int items = un.nk * S;
+      for (int q = t; q < items; q += T) seam_item<N>(f.u, c, q, touch);
+    } else {
+      seam_plane_point(f, id - threads, touch);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int seam_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int E, int mode,
+                            double *u, int nsteps, char *err, int errlen)
+{
+  Err e;
+  FieldDesc f{};
+  f.n = n;
+  f.m[0] = mx; f.m[1] = my; f.m[2] = mz;
+  f.L[0] = lx; f.L[1] = ly; f.L[2] = lz;
+  f.periodic = periodic;
+  f.mode = kDirect;
+  f.nranks = lx * ly * lz;
+  f.sjy = (long)n * n * n * mx;
+  f.sjz = jz_stride(n, mx, my);
+  f.R = f.sjz * mz;
+  const long total = f.R * f.nranks;
+  std::vector<int> nbr = neighbour_table(f.L, periodic != 0);
+  f.nbr = nbr.data();
+  std::vector<double> field(total + 2 * kGuard, kSentinel);
+  f.u = field.data() + kGuard;
+  std::memcpy(f.u, u, sizeof(double) * total);
+  if (E < 1 || E > mx) E = mx;
+  for (int step = 0; step < nsteps && e.ok; step++) {
+    switch (n) {
+      case 2: seam_share<2>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 3: seam_share<3>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 4: seam_share<4>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 5: seam_share<5>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 6: seam_share<6>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 7: seam_share<7>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 8: seam_share<8>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 9: seam_share<9>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 10: seam_share<10>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 11: seam_share<11>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 12: seam_share<12>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      case 16: seam_share<16>(f, E, (mode & 1) != 0, (mode & 2) != 0, e); break;
+      default: e.set("n not replayed", -1);
+    }
+    if (!guards_intact(field, total)) e.set("guard cells changed", -1);
+  }
+  std::memcpy(u, f.u, sizeof(double) * total);
+  if (!e.ok) {
+    snprintf(err, errlen, "%s", e.msg.c_str());
+    return -1;
+  }
+  return 0;
+}

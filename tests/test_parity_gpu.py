@@ -18,9 +18,11 @@ if not torch.cuda.is_available():
 
 
 def run_gpu(F, s, *, periodic, messages, gather=False, rows=False, general=False, init="int", seed=5, nsteps=2,
-            compute=True):
+            compute=True, seams=False, tune=None):
     f = F.Faces(s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n, periodic=periodic, messages=messages, gather=gather,
-                rows=rows, general=general)
+                rows=rows, general=general, seams=seams)
+    if tune:
+        f.set_tuning(**tune)
     u = f.field()
     if init == "int":
         f.init_int(u, seed)
@@ -55,17 +57,21 @@ SHAPES = [
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
 @pytest.mark.parametrize("messages", [False, True], ids=["direct", "messages"])
-@pytest.mark.parametrize("kernel", ["tiles", "general", "rows"])
+@pytest.mark.parametrize("kernel", ["tiles", "general", "rows", "seams", "seams-lean"])
 def test_step_bit_exact(oracle, faces_lib, shape, periodic, messages, kernel):
     """tiles: the periodic tile step where it applies (periodic direct mode),
-    else the general one; general: the general tile step everywhere."""
+    else the general one; general: the general tile step everywhere; seams:
+    the seam kernel (direct mode only), one launch or split in two."""
     O, F = oracle, faces_lib
     if kernel == "general" and not (periodic and not messages):
         pytest.skip("same kernel as 'tiles' here")
+    if kernel.startswith("seams") and messages:
+        pytest.skip("the seam kernel sums in place (direct mode)")
     s = O.Shape(*shape, periodic=periodic)
     for init in ("int", "ref"):
         u_init, out, chk = run_gpu(F, s, periodic=periodic, messages=messages, rows=kernel == "rows",
-                                   general=kernel == "general", init=init, nsteps=3)
+                                   general=kernel == "general", init=init, nsteps=3, seams=kernel.startswith("seams"),
+                                   tune={"order": 1} if kernel == "seams-lean" else None)
         ref0 = O.init_int(s, 5) if init == "int" else O.init_ref(s)
         assert np.array_equal(u_init, ref0), "device init differs from the host formula"
         exp = O.groups_share(s, ref0.copy(), True, 3)
@@ -105,13 +111,15 @@ def test_mugs_bit_exact_single_rank(oracle, faces_lib):
 
 
 @pytest.mark.parametrize("chunk", [1, 2, 3, 5, 8, 16])
-@pytest.mark.parametrize("kernel", ["tiles", "general", "rows"])
+@pytest.mark.parametrize("kernel", ["tiles", "general", "rows", "seams"])
 def test_chunking(oracle, faces_lib, chunk, kernel):
     O, F = oracle, faces_lib
     for periodic, messages in itertools.product([False, True], [False, True]):
+        if kernel == "seams" and messages:
+            continue
         s = O.Shape(2, 1, 1, 7, 2, 2, 5, periodic=periodic)
         f = F.Faces(*((s.lx, s.ly, s.lz, s.mx, s.my, s.mz, s.n)), periodic=periodic, messages=messages,
-                    rows=kernel == "rows", general=kernel == "general")
+                    rows=kernel == "rows", general=kernel == "general", seams=kernel == "seams")
         f.set_tuning(chunk=chunk, width=1 + chunk % 3, order=[0, 1, 2, 2 + 16][chunk % 4])
         u = f.field()
         f.init_ref(u)
@@ -215,7 +223,7 @@ def test_warp_tiles_bit_exact(oracle, faces_lib, shape):
                                    (3, 1, 1, 6, 9, 8, 9), (1, 1, 1, 24, 5, 6, 3), (3, 3, 3, 16, 16, 16, 6)],
                          ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
-@pytest.mark.parametrize("mode", ["tiles", "general", "rows", "messages", "v6"])
+@pytest.mark.parametrize("mode", ["tiles", "general", "rows", "messages", "v6", "seams", "seams-lean"])
 def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
     """The reference's 15x14x13 n=12 shape, the 3x3x3-rank 16^3 n=6 grid at
     full size, and other shapes with every dimension several elements long,
@@ -225,7 +233,9 @@ def test_larger_shapes_closed_form(faces_lib, shape, periodic, mode):
     outs = []
     for m in ("tiles", mode):
         f = F.Faces(*shape, periodic=periodic, general=m == "general", rows=m == "rows",
-                    messages=m == "messages", v6=m == "v6")
+                    messages=m == "messages", v6=m == "v6", seams=m.startswith("seams"))
+        if m == "seams-lean":
+            f.set_tuning(order=1)
         u = f.field()
         f.init_int(u, 9)
         f.share_n(u, 3)

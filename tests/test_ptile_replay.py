@@ -225,3 +225,63 @@ def test_v6_replay_matches_oracle(oracle, case, fused, compute):
     assert rc == 0, err.value.decode()
     exp = O.v6_share(s, u0.copy(), compute, 2)
     assert np.array_equal(u, exp), f"{np.count_nonzero(u != exp)} points differ"
+
+
+_semu = None
+
+
+def semu():
+    global _semu
+    if _semu is None:
+        L = ctypes.CDLL(build_emu.build_ptile())
+        L.seam_emulate.argtypes = [ctypes.c_int] * 10 + [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                                         ctypes.c_char_p, ctypes.c_int]
+        L.seam_emulate.restype = ctypes.c_int
+        _semu = L
+    return _semu
+
+
+def seam_default_chunk(n):
+    """the seam kernel's default chunk: about eight slots per thread of a
+    256-thread block"""
+    return max(1, 8 * 256 // (n - 1) ** 2)
+
+
+SEAMGRIDS = [
+    # lx ly lz mx my mz periodic
+    (1, 1, 1, 4, 3, 2, True),
+    (1, 1, 1, 4, 3, 2, False),
+    (2, 1, 2, 3, 2, 2, True),
+    (2, 2, 1, 3, 2, 1, False),
+    (3, 2, 2, 2, 1, 2, False),
+    (2, 2, 2, 1, 1, 1, True),
+]
+
+
+@pytest.mark.parametrize("n", list(range(2, 13)) + [16])
+@pytest.mark.parametrize("grid", SEAMGRIDS, ids=lambda g: "x".join(map(str, g[:6])) + ("p" if g[6] else "o"))
+@pytest.mark.parametrize("E", [1, 3, 0], ids=["E1", "E3", "Ewhole"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["fwd", "rev", "lean", "lean-rev"])
+def test_seam_replay_matches_oracle(oracle, n, grid, E, mode):
+    """The seam step in both forms (chunked; lean, with the boundary planes'
+    launch), every thread run one by one, in order or in reverse: no point is
+    touched by two threads of a share, no address leaves the field, and 2
+    shares equal the oracle bit for bit (random normal inputs)."""
+    O = oracle
+    *shape, periodic = grid
+    s = O.Shape(*shape, n, periodic=periodic)
+    rng = np.random.default_rng(n * 100 + sum(shape))
+    u0 = O.init_int(s, 3)
+    m = u0 != 0
+    u0[m] = rng.standard_normal(m.sum())
+    u = u0.copy()
+    err = ctypes.create_string_buffer(256)
+    rc = semu().seam_emulate(*shape, n, int(periodic), E, mode,
+                             u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, err, 256)
+    assert rc == 0, err.value.decode()
+    exp = O.groups_share(s, u0.copy(), True, 2)
+    assert np.array_equal(u, exp), f"{np.count_nonzero(u != exp)} points differ"
+
+
+def test_seam_default_chunk():
+    assert [seam_default_chunk(n) for n in (2, 4, 8, 12, 16)] == [2048, 227, 41, 16, 9]
