@@ -1,7 +1,8 @@
 """Run the reference's own CUDA executables and this repository's `faces`
 executable on the same stdin, on one GPU, and print one JSON line per run.
 
-    python baseline/run_gpu.py [--quick] [--out FILE]
+    python baseline/run_gpu.py [--quick] [--out FILE] [--argset NAME] [--variant V --threads T]
+                               [--faces-only] [--faces-options OPT]
 
 The reference's executables come from `make -C baseline gpu` (built here from
 the staged, unmodified sources in baseline/_ref/src if they are missing).
@@ -14,8 +15,10 @@ its result on the device against the closed form.
 GB/s counts 16 bytes per field point per timed share (each point read and
 written once), the same algorithmic bytes for every implementation.
 
-Argument sets: the reference's own (gpu/frontier-run-all-1.sh:15,17) and the
-48^3 n=8 roofline field.
+Argument sets: the reference's own (gpu/frontier-run-all-1.sh:15,17), the
+48^3 n=8 roofline field, and a 40^3 n=12 field (885 MB: above L2, small
+enough for a full ncu capture of one launch).  --argset, --variant, --threads
+and --faces-options select one run each (for profiling under ncu).
 """
 from __future__ import annotations
 
@@ -37,6 +40,7 @@ ARGSETS = {
     "15x14x13_n12": "1 1 1 15 14 13 12 10 10 100",
     "95x94x93_n12": "1 1 1 95 94 93 12 3 1 10",
     "48cubed_n8": "1 1 1 48 48 48 8 1 1 100",
+    "40cubed_n12": "1 1 1 40 40 40 12 1 1 3",
 }
 VARIANTS = ["v26-inner", "v26-all", "v6-basic"]
 THREADS = [32, 256, 1024]
@@ -76,19 +80,37 @@ def main() -> None:
     ap.add_argument("--out", default="")
     ap.add_argument("--timeout", type=float, default=300.0)
     ap.add_argument("--faces-only", action="store_true", help="run only this repository's executable")
+    ap.add_argument("--argset", choices=list(ARGSETS), help="run this argument set only")
+    ap.add_argument("--variant", choices=VARIANTS, help="run this reference build only")
+    ap.add_argument("--threads", type=int, choices=THREADS, help="run this MAXTHREADS only")
+    ap.add_argument("--faces-options", choices=["default", "--autotune", "--messages", "--v6", "none"],
+                    help="run the faces executable with these options only (none: not at all)")
     args = ap.parse_args()
+    if args.argset:
+        for k in [k for k in ARGSETS if k != args.argset]:
+            del ARGSETS[k]
+    if args.variant:
+        VARIANTS[:] = [args.variant]
     if args.faces_only:
         VARIANTS.clear()
     elif not os.path.isfile(SRC):
         print(json.dumps({"unavailable": "the reference sources are not staged in baseline/_ref/src "
                                          "(make -C baseline stage, where the reference is present)"}))
         return
-    r = subprocess.run(["make", "-C", HERE, "-s", f"-j{os.cpu_count() or 4}", "gpu"], capture_output=True, text=True)
+    threads = [args.threads] if args.threads else [256] if args.quick else THREADS
+    # build what runs: every reference build, or the one selected
+    targets = ([os.path.join(BIN, f"faces-{v}-t{t}") for v in VARIANTS for t in threads]
+               if args.variant or args.threads else ["gpu"])
+    r = subprocess.run(["make", "-C", HERE, "-s", f"-j{os.cpu_count() or 4}", *targets], capture_output=True,
+                       text=True) if VARIANTS else None
     if VARIANTS and r.returncode != 0:
         print(json.dumps({"unavailable": "reference build failed: " + (r.stdout + r.stderr)[-400:]}))
         return
     lines = []
-    threads = [256] if args.quick else THREADS
+    faces_opts = ([], ["--autotune"], ["--messages"], ["--v6"])
+    if args.faces_options:
+        faces_opts = () if args.faces_options == "none" else \
+            ([],) if args.faces_options == "default" else ([args.faces_options],)
     for name, stdin in ARGSETS.items():
         for v in VARIANTS:
             for t in threads:
@@ -97,7 +119,7 @@ def main() -> None:
                 rec.update(run_one([exe], stdin + "\n", args.timeout))
                 lines.append(rec)
                 print(json.dumps(rec), flush=True)
-        for opts in ([], ["--autotune"], ["--messages"], ["--v6"]):
+        for opts in faces_opts:
             rec = {"impl": "faces_gb300", "options": " ".join(opts) or "(default)", "args": name, "stdin": stdin}
             rec.update(run_one([FACES, *opts], stdin + "\n", args.timeout))
             lines.append(rec)

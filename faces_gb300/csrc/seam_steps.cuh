@@ -451,22 +451,10 @@ FACES_HD void seam_plane_point(const FieldDesc &f, long p, Touch touch = Touch()
 
 FACES_HD constexpr int seam_lean_slots(int n) { return n > 2 ? (n - 2) * (n - 2) : 1; }
 
-// element e of the field (x fastest, then y, z, rank)
+// an element of the field
 struct SeamElem {
   int r, jx, jy, jz;
 };
-
-FACES_HD SeamElem seam_elem(const FieldDesc &f, long e)
-{
-  SeamElem el;
-  el.jx = (int)(e % f.m[0]);
-  e /= f.m[0];
-  el.jy = (int)(e % f.m[1]);
-  e /= f.m[1];
-  el.jz = (int)(e % f.m[2]);
-  el.r = (int)(e / f.m[2]);
-  return el;
-}
 
 // The element (jx+dx, jy+dy, jz+dz) of rank r, dx, dy, dz in {-1, 0}, and
 // whether it exists (a lower index of -1 is the lower neighbour rank's last
@@ -579,16 +567,21 @@ FACES_HD void seam_corner(const FieldDesc &f, const SeamElem &el, Touch touch)
   }
 }
 
-// lean item g: element g / seam_lean_slots(n), slot (a, b) in [1, n-2]^2 with
-// a fastest
+// lean item t of column col (rank, jz, jy; jy fastest): element t /
+// seam_lean_slots(n) of the column, slot (a, b) in [1, n-2]^2 with a fastest
+// (32-bit decoding: a column holds at most 2^31 items)
 template <int N, class Touch = NoTouch>
-FACES_HD void seam_lean_item(const FieldDesc &f, long g, Touch touch = Touch())
+FACES_HD void seam_lean_item(const FieldDesc &f, int col, int t, Touch touch = Touch())
 {
   constexpr int W = N - 2, F = seam_lean_slots(N);
   constexpr long NN = (long)N * N;
-  const long e = g / F;
-  const int s = (int)(g - e * F);
-  const SeamElem el = seam_elem(f, e);
+  SeamElem el;
+  el.jy = col % f.m[1];
+  const int rest = col / f.m[1];
+  el.jz = rest % f.m[2];
+  el.r = rest / f.m[2];
+  el.jx = t / F;
+  const int s = t - el.jx * F;
   const long own = (long)el.r * f.R + (long)el.jz * f.sjz + (long)el.jy * f.sjy + (long)el.jx * (N * NN);
   if constexpr (W <= 0) {
     (void)s;

@@ -36,12 +36,15 @@ __global__ void __launch_bounds__(kSeamThreads, 4) seam_kernel(FieldDesc f, int 
     seam_plane_point(f, p);
 }
 
-// lean: one face slot per thread (with its edge points)
+// lean: one face slot per thread (with its edge points); blockIdx.x is the
+// position along the column, so that consecutive blocks take consecutive
+// elements of one column (an element's x-lower neighbour is still in cache),
+// and blockIdx.y + gridDim.y * blockIdx.z the column (rank, jz, jy)
 template <int N>
-__global__ void __launch_bounds__(kSeamThreads, 6) seam_lean_kernel(FieldDesc f, long items)
+__global__ void __launch_bounds__(kSeamThreads, 6) seam_lean_kernel(FieldDesc f, int per_column)
 {
-  const long g = (long)blockIdx.x * kSeamThreads + threadIdx.x;
-  if (g < items) seam_lean_item<N>(f, g);
+  const int t = blockIdx.x * kSeamThreads + threadIdx.x;
+  if (t < per_column) seam_lean_item<N>(f, (int)(blockIdx.y + gridDim.y * blockIdx.z), t);
 }
 
 // lean: the open boundary planes
@@ -75,8 +78,17 @@ template <int N>
 cudaError_t launch_n(const FieldDesc &f, const SeamPlan &p, cudaStream_t s)
 {
   if (p.lean) {
-    const long items = (long)f.nranks * f.m[0] * f.m[1] * f.m[2] * seam_lean_slots(N);
-    seam_lean_kernel<N><<<(unsigned)blocks_for(items, 0x7fffffffL), kSeamThreads, 0, s>>>(f, items);
+    // columns as y (up to 65535) times z: cols = gy * gz exactly
+    const long cols = (long)f.nranks * f.m[1] * f.m[2];
+    const long per_column = (long)f.m[0] * seam_lean_slots(N);
+    const long xs = (per_column + kSeamThreads - 1) / kSeamThreads;
+    long gy = cols, gz = 1;
+    if (cols > 65535) {
+      gy = f.m[1];
+      gz = cols / f.m[1];
+    }
+    if (gy > 65535 || gz > 65535 || per_column > 0x7fffffffL) return cudaErrorInvalidConfiguration;
+    seam_lean_kernel<N><<<dim3((unsigned)xs, (unsigned)gy, (unsigned)gz), kSeamThreads, 0, s>>>(f, (int)per_column);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.plane_items == 0) return e;
     seam_plane_kernel<<<(unsigned)blocks_for(p.plane_items, 1L << 16), kSeamThreads, 0, s>>>(f, p.plane_items);

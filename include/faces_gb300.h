@@ -77,7 +77,7 @@ extern "C" {
                                direct mode only (not with FACES_MESSAGES,
                                FACES_V6 or FACES_V6F).  Without it the seam
                                kernel is still the default for direct-mode
-                               fields with n >= 12 (FACES_ROWS and
+                               fields with n >= 11 (FACES_ROWS and
                                FACES_GENERAL keep theirs). */
 
 typedef struct faces_ctx faces_ctx;
@@ -159,7 +159,7 @@ int faces_run_host_many(faces_ctx *ctx, int njobs, const double *const *u_in, do
  * over units of u consecutive x-chunks of a column, listed chunk group first,
  * u = 0 half a column; 3: periodic step only, one warp per tile instead of
  * one block, no block barriers).  With the seam kernel (FACES_SEAMS, and
- * the default for direct-mode fields with n >= 12): elements per x-chunk of
+ * the default for direct-mode fields with n >= 11): elements per x-chunk of
  * its chunked form, resident blocks per SM, and the form (order 0 chunked,
  * 1 lean: one thread per face slot of every element, plus a launch for the
  * open boundary planes; < 0: lean where the field gives four waves of

@@ -547,12 +547,13 @@ namespace {
 template <int N, class T>
 void seam_lean_share(const FieldDesc &f, bool reverse, long &who, T touch, Err &e)
 {
-  const long items = (long)f.nranks * f.m[0] * f.m[1] * f.m[2] * seam_lean_slots(N);
+  const int cols = f.nranks * f.m[1] * f.m[2], per = f.m[0] * seam_lean_slots(N);
+  const long items = (long)cols * per;
   const long planes = f.periodic ? 0 : (long)f.nranks * seam_plane_items(f);
   for (long k = 0; k < items && e.ok; k++) {
     const long g = reverse ? items - 1 - k : k;
     who = g;
-    seam_lean_item<N>(f, g, touch);
+    seam_lean_item<N>(f, (int)(g / per), (int)(g % per), touch);
   }
   for (long k = 0; k < planes && e.ok; k++) {
     const long g = reverse ? planes - 1 - k : k;
