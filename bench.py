@@ -459,9 +459,10 @@ def reference_gpu_leg(timeout: float = 240.0) -> dict:
     """The reference's gpu/main.cc with v-26 Faces.cc (FUSE_SEND, FUSE_INNER,
     FUSE_RECV; MAXTHREADS 256), unmodified, built for sm_103a against a
     one-rank MPI stand-in, on `1 1 1 48 48 48 8 1 1 100` -- the roofline
-    field in the reference's open mode -- and this repository's `faces`
-    executable on the same stdin.  Each prints the reference's `time` and
-    `tasks passed` lines; GB/s = 16 B per point per timed share."""
+    field in the reference's open mode -- and on the reference's own two
+    argument sets (gpu/frontier-run-all-1.sh:15,17), and this repository's
+    `faces` executable on the same stdin.  Each prints the reference's `time`
+    and `tasks passed` lines; GB/s = 16 B per point per timed share."""
     sys.path.insert(0, os.path.join(ROOT, "baseline"))
     import run_gpu as RG
     stdin = RG.ARGSETS["48cubed_n8"] + "\n"
@@ -480,6 +481,18 @@ def reference_gpu_leg(timeout: float = 240.0) -> dict:
            "faces_gb300": dict(ours, build="faces executable, default settings")}
     if ref.get("ok") and ours.get("ok"):
         out["speedup"] = round(ref["time_s"] / ours["time_s"], 2)
+    # the reference's own argument sets, same two executables
+    shapes = {}
+    for name in ("15x14x13_n12", "95x94x93_n12"):
+        stdin = RG.ARGSETS[name] + "\n"
+        r, o = RG.run_one([exe], stdin, timeout), RG.run_one([RG.FACES], stdin, timeout)
+        rec = {"stdin": stdin.strip(), "reference_gbs": r.get("gbs"), "faces_gb300_gbs": o.get("gbs"),
+               "reference_ok": bool(r.get("ok") and r.get("tasks_passed") == 1),
+               "faces_gb300_ok": bool(o.get("ok") and o.get("tasks_passed") == 1)}
+        if r.get("ok") and o.get("ok"):
+            rec["speedup"] = round(r["time_s"] / o["time_s"], 2)
+        shapes[name] = rec
+    out["reference_shapes"] = shapes
     return out
 
 

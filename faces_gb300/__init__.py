@@ -337,8 +337,9 @@ class Faces:
         return _check(lib().faces_autotune(self._h, _ptr(u), int(compute), trials, _stream(stream)))
 
     def tuning(self) -> dict:
-        """The step's settings: elements per tile, chunks per unit, blocks, and
-        the kernel (0 tile step, 1 general tile step, 2 row kernel)."""
+        """The step's settings: elements per tile, chunks per unit, blocks, the
+        kernel (0 tile step, 1 general tile step, 2 row kernel, 3 seam kernel)
+        and the order (seam kernel: 0 chunked, 1 lean)."""
         v = [ctypes.c_int() for _ in range(5)]
         _check(lib().faces_get_tuning(self._h, *[ctypes.byref(x) for x in v]))
         return dict(zip(("chunk", "unit_chunks", "blocks", "kernel", "order"), (x.value for x in v)))

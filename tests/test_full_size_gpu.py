@@ -25,8 +25,10 @@ if not torch.cuda.is_available():
     pytest.skip("no CUDA device", allow_module_level=True)
 
 
-def run(F, shape, nshares, *, periodic=True, init="int", seed=11, autotune=False, **mode):
+def run(F, shape, nshares, *, periodic=True, init="int", seed=11, autotune=False, tune=None, **mode):
     f = F.Faces(*shape, periodic=periodic, **mode)
+    if tune:
+        f.set_tuning(**tune)
     u = f.field()
     if init == "int":
         f.init_int(u, seed)
@@ -76,16 +78,40 @@ def test_c3_full_size_equals_oracle(oracle, faces_lib, mode):
         assert np.array_equal(out, expected(oracle, C3, 3)), "v-6 differs from the group sums"
 
 
-@pytest.mark.parametrize("mode", ["direct", "messages", "v6", "v6f"])
+@pytest.mark.parametrize("mode", ["direct", "seams-lean", "general", "messages", "v6", "v6f"])
 def test_reference_shape_open_equals_oracle(oracle, faces_lib, mode):
     """The reference's own argument set 1 1 1 15 14 13 12 (open, reference
-    init, 2 shares): the same tree order as Mugs, so equal on any input."""
+    init, 2 shares): the same tree order as Mugs, so equal on any input.
+    direct: the default (the seam kernel's chunked form at this size);
+    seams-lean: its lean form; general: the general tile step."""
     shape = (1, 1, 1, 15, 14, 13, 12)
     exp = expected(oracle, shape, 2, periodic=False, init="ref", v6=mode.startswith("v6"))
     out, chk = run(faces_lib, shape, 2, periodic=False, init="ref", messages=mode == "messages", v6=mode == "v6",
-                   v6f=mode == "v6f")
+                   v6f=mode == "v6f", general=mode == "general", seams=mode == "seams-lean",
+                   tune={"order": 1} if mode == "seams-lean" else None)
     assert np.array_equal(out, exp), f"{np.count_nonzero(out != exp)} points differ"
     assert chk.passed
+
+
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+def test_reference_large_shape_seams_equal_tiles(faces_lib, periodic):
+    """The reference's 1 1 1 95 94 93 12 shape (1.4 G points) at full size,
+    2 shares: the default (the seam kernel's lean form) equals the general
+    tile step bit for bit on the device, and the device check passes."""
+    F = faces_lib
+    shape = (1, 1, 1, 95, 94, 93, 12)
+    outs = []
+    for general in (False, True):
+        f = F.Faces(*shape, periodic=periodic, general=general)
+        assert (f.tuning()["kernel"] == 3) != general
+        u = f.field()
+        f.init_ref(u)
+        f.share_n(u, 2)
+        chk = f.check(u, init="ref", nshares=2)
+        assert chk.passed and chk.npass == 1, (general, chk)
+        outs.append(u)
+        f.close()
+    assert torch.equal(outs[0], outs[1])
 
 
 # -- faces_check must fail where the field is wrong --------------------------
