@@ -377,15 +377,35 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   CUDA_TRY(cudaEventCreate(&e1), "autotune: event");
   float best = 1e30f;
   int bk = c->chunk, bo = c->order, bw = c->tpb, bv = c->variant, applied = 0, rc = FACES_OK;
+  // shares per trial: at least `trials`, and enough for about 1 ms (the
+  // current settings' share time, measured once), so that short shares are
+  // not timed by their launch overhead and noise
+  int reps = trials;
+  {
+    replan(*c);
+    if ((rc = share_once(c, u, compute, s)) == FACES_OK) {
+      cudaEventRecord(e0, s);
+      for (int t = 0; t < trials && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
+      cudaEventRecord(e1, s);
+      applied += 1 + trials;
+    }
+    float ms = 0;
+    if (rc == FACES_OK && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+        ms > 0) {
+      const float per = ms / trials;
+      const int want = (int)(1.0f / per) + 1;
+      reps = want < trials ? trials : (want > 200 ? 200 : want);
+    }
+  }
   // time the current settings (kernel variant v) once; keep the fastest
   auto trial = [&](int v) {
     c->variant = v;
     replan(*c);
     if ((rc = share_once(c, u, compute, s))) return;  // warm-up
     cudaEventRecord(e0, s);
-    for (int t = 0; t < trials && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
+    for (int t = 0; t < reps && rc == FACES_OK; t++) rc = share_once(c, u, compute, s);
     cudaEventRecord(e1, s);
-    applied += 1 + trials;
+    applied += 1 + reps;
     if (rc) return;
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess) {
@@ -419,11 +439,12 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   if (rc == FACES_OK && !periodic_step && !(c->flags & FACES_GENERAL)) trial(1);
   if (rc == FACES_OK && row_kernel_supported(c->n)) trial(2);
   // the seam kernel (direct mode): the chunked form (order 0) at its
-  // default chunk and twice it, and the lean form (order 1)
+  // default chunk (shortened for small fields) and at twice the unshortened
+  // one, and the lean form (order 1)
   if (!(c->flags & FACES_MESSAGES) && seam_kernel_supported(c->n)) {
     const int e0 = seam_default_chunk(c->n);
     c->order = 0;
-    for (int e : {e0, 2 * e0}) {
+    for (int e : {0, 2 * e0}) {
       if (rc != FACES_OK) break;
       c->chunk = e;
       trial(3);

@@ -169,11 +169,11 @@ int faces_set_tuning(faces_ctx *ctx, int chunk, int width, int order);
 /* Times the tile step on the field u over elements per tile (default, half,
  * double), units (half a column, one chunk, warp tiles) and resident blocks
  * per SM (default, 2), the general tile step and the row kernel at their
- * defaults, and in direct mode the seam kernel (chunked at two chunk
- * lengths; lean), `trials` shares each after one warm-up, and keeps the
- * fastest
+ * defaults, and in direct mode the seam kernel (chunked at its default and
+ * at a longer chunk; lean), each after one warm-up over at least `trials`
+ * shares and at least about 1 ms of shares, and keeps the fastest
  * (faces_set_tuning's settings and the kernel; faces_set_tuning returns to
- * the tile step).  Every timed launch is a share of
+ * the default kernel).  Every timed launch is a share of
  * u: returns how many it applied (>= 0; re-initialise u afterwards) or an
  * error code.  The reference fixes these choices at compile time
  * (MAXTHREADS, gpu/gpu.h:185-200).  Synchronous. */

@@ -147,12 +147,14 @@ def test_large_field_properties(oracle, faces_lib, kernel):
     assert torch.equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("shape", [(1, 1, 1, 9, 7, 5, 8), (2, 1, 2, 5, 3, 4, 5), (1, 2, 1, 6, 4, 3, 10)],
+@pytest.mark.parametrize("shape", [(1, 1, 1, 9, 7, 5, 8), (2, 1, 2, 5, 3, 4, 5), (1, 2, 1, 6, 4, 3, 10),
+                                   (1, 1, 1, 6, 5, 4, 12), (2, 1, 1, 3, 4, 2, 11)],
                          ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
 def test_autotune_keeps_results(oracle, faces_lib, shape, periodic):
-    """faces_autotune times several tile settings on the field and keeps one;
-    every setting it can pick must give the oracle's result."""
+    """faces_autotune times several tile settings (and, at n >= 11 in direct
+    mode, the seam kernel's forms) on the field and keeps one; every setting
+    it can pick must give the oracle's result."""
     O, F = oracle, faces_lib
     s = O.Shape(*shape, periodic=periodic)
     f = F.Faces(*shape, periodic=periodic)
