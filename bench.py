@@ -419,12 +419,14 @@ def c3_leg(F, dev) -> dict:
     stream = torch.cuda.current_stream(dev)
     peak, peak_kind = hbm_peak()
     modes = {}
-    for mode in ("messages", "direct", "v6", "v6f"):
-        f = F.Faces(*C3_SHAPE, periodic=True, messages=mode == "messages", v6=mode == "v6", v6f=mode == "v6f")
+    for mode in ("messages", "messages-fused", "direct", "v6", "v6f"):
+        f = F.Faces(*C3_SHAPE, periodic=True, messages=mode.startswith("messages"), v6=mode == "v6", v6f=mode == "v6f",
+                    pack_fused=mode == "messages-fused")
         u = f.field(dev)
         f.init_int(u, SEED, stream)
         if not mode.startswith("v6"):
             f.autotune(u, True, 3, stream)
+        status = f.status() if mode == "messages-fused" else 0
         f.init_int(u, SEED, stream)
         for _ in range(3):
             f.share(u, True, stream)
@@ -437,7 +439,9 @@ def c3_leg(F, dev) -> dict:
                        "field_gbs": round(16 * f.points / (ms * 1e-3) / 1e9, 1),
                        "frac": round(b / (ms * 1e-3) / 1e9 / peak, 4), "bytes_per_share": b,
                        "message_doubles": msg, "launches_per_share": f.launches_per_share(True),
-                       "tuning": f.tuning(), "check_passed": bool(chk.passed and chk.maxrel == 0.0)}
+                       "tuning": f.tuning(),
+                       "check_passed": bool(chk.passed and chk.maxrel == 0.0 and status == 0 and
+                                            (mode != "messages-fused" or f.status() == 0))}
         del u
         f.close()
     torch.cuda.empty_cache()

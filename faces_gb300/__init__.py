@@ -30,6 +30,7 @@ GENERAL = 0x10
 V6 = 0x20
 V6F = 0x40
 SEAMS = 0x80
+PACK_FUSED = 0x100
 
 _ERRNAMES = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "EALIGN", -5: "EUNSUPPORTED"}
 
@@ -72,6 +73,7 @@ def lib() -> ctypes.CDLL:
     L.faces_run_host_many.restype = c_int
     L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
+    L.faces_status.argtypes = [vp, ctypes.POINTER(c_int)]
     L.faces_autotune.argtypes = [vp, dp, c_int, c_int, vp]
     L.faces_autotune.restype = c_int
     L.faces_get_tuning.argtypes = [vp] + [ctypes.POINTER(c_int)] * 5
@@ -213,20 +215,25 @@ class Faces:
                 Faces.cc: four launches per share, the same results as v6
     seams    -- the seam kernel: one thread per shared point of each
                 element's lower seam planes, no shared memory (direct mode)
+    pack_fused -- message mode: the pack in the message-mode tile kernel's
+                prologue, one cooperative launch per share (by default the
+                pack is its own launch)
     """
 
     def __init__(self, lx: int, ly: int, lz: int, mx: int, my: int, mz: int, n: int, *,
                  periodic: bool = False, messages: bool = False, gather: bool = False, rows: bool = False,
-                 general: bool = False, v6: bool = False, v6f: bool = False, seams: bool = False):
+                 general: bool = False, v6: bool = False, v6f: bool = False, seams: bool = False,
+                 pack_fused: bool = False):
         flags = ((PERIODIC if periodic else 0) | (MESSAGES if messages else 0) | (GATHER if gather else 0)
                  | (ROWS if rows else 0) | (GENERAL if general else 0) | (V6 if v6 else 0) | (V6F if v6f else 0)
-                 | (SEAMS if seams else 0))
+                 | (SEAMS if seams else 0) | (PACK_FUSED if pack_fused else 0))
         h = ctypes.c_void_p()
         _check(lib().faces_create(ctypes.byref(h), lx, ly, lz, mx, my, mz, n, flags))
         self._h = h
         self.shape = (lx, ly, lz, mx, my, mz, n)
         self.periodic, self.messages, self.gather, self.rows = periodic, messages, gather, rows
         self.general, self.v6, self.v6f, self.seams = general, v6, v6f, seams
+        self.pack_fused = pack_fused
         s = (ctypes.c_long * 6)()
         rd, tot = ctypes.c_long(), ctypes.c_long()
         _check(lib().faces_layout(h, s, ctypes.byref(rd), ctypes.byref(tot)))
@@ -347,6 +354,13 @@ class Faces:
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))
 
+    def status(self) -> int:
+        """Device status bits, read and cleared (synchronous): bit 0 = the
+        fused message-mode step's wait for the pack ran out."""
+        b = ctypes.c_int()
+        _check(lib().faces_status(self._h, ctypes.byref(b)))
+        return b.value
+
 
 class Batch:
     """Many independent fields advanced together (no counterpart in the
@@ -370,7 +384,7 @@ class Batch:
         flags = ((PERIODIC if faces.periodic else 0) | (MESSAGES if faces.messages else 0)
                  | (GATHER if faces.gather else 0) | (ROWS if faces.rows else 0)
                  | (GENERAL if faces.general else 0) | (V6 if faces.v6 else 0) | (V6F if faces.v6f else 0)
-                 | (SEAMS if faces.seams else 0))
+                 | (SEAMS if faces.seams else 0) | (PACK_FUSED if faces.pack_fused else 0))
         fid = ctypes.c_int()
         _check(lib().faces_batch_add(self._h, _ptr(u), lx, ly, lz, mx, my, mz, n, flags, ctypes.byref(fid)))
         self._fields.append(u)

@@ -25,6 +25,7 @@ struct faces_ctx {
   long *d_roff = nullptr;
   double *d_msg = nullptr;
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
+  unsigned long long *d_sync = nullptr;     // fused pack: [0] arrivals, [1] the wait's error bits
   double *d_field = nullptr;                // faces_run_host's device copy
   // faces_run_host_many: a second device field, copy streams and the events
   // that order uploads, shares and downloads of the two fields

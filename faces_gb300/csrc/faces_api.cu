@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/faces_gb300.h"
+#include "pack_steps.cuh"
 #include "geom.cuh"
 #include "kernels.cuh"
 #include "tables.h"
@@ -80,6 +81,15 @@ bool seam_step(const faces_ctx &c)
 {
   return (c.variant == 3 || (c.flags & FACES_SEAMS)) && seam_kernel_supported(c.n) &&
          !(c.flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F | FACES_GATHER));
+}
+
+// message mode with FACES_PACK_FUSED: the pack runs in the message-mode
+// tile kernel's prologue (one launch per share) when that kernel runs
+bool pack_in_tiles(const faces_ctx &c, int compute)
+{
+  const bool general = (c.flags & FACES_GENERAL) || c.variant == 1;
+  return (c.flags & FACES_MESSAGES) && (c.flags & FACES_PACK_FUSED) && !(c.flags & (FACES_GATHER | FACES_ROWS)) &&
+         compute && !general && c.variant == 0 && c.tplan.order != 3 && tile_kernel_supported(c.n);
 }
 
 // The default kernel: the seam kernel for direct-mode fields with n >= 11,
@@ -173,7 +183,7 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
   if (mx < 1 || my < 1 || mz < 1) return fail(FACES_EINVAL, "element grid %d x %d x %d must be positive", mx, my, mz);
   if (n < 2) return fail(FACES_EINVAL, "element size n = %d: n must be at least 2", n);
   if (flags & ~(FACES_PERIODIC | FACES_MESSAGES | FACES_GATHER | FACES_ROWS | FACES_GENERAL | FACES_V6 | FACES_V6F |
-                FACES_SEAMS))
+                FACES_SEAMS | FACES_PACK_FUSED))
     return fail(FACES_EINVAL, "unknown flags 0x%x", flags);
   if ((flags & FACES_SEAMS) && (flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F)))
     return fail(FACES_EINVAL, "FACES_SEAMS sums every copy in place: not with a message strategy");
@@ -202,6 +212,8 @@ int faces_create(faces_ctx **out, int lx, int ly, int lz, int mx, int my, int mz
       (e = cudaMalloc(&c->d_off, sizeof(long) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_roff, sizeof(long) * nranks * 27)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_scratch, sizeof(unsigned long long) * (nranks + 4))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_sync, sizeof(unsigned long long) * 2)) != cudaSuccess ||
+      (e = cudaMemset(c->d_sync, 0, sizeof(unsigned long long) * 2)) != cudaSuccess ||
       (c->msg_total > 0 && (e = cudaMalloc(&c->d_msg, sizeof(double) * c->msg_total)) != cudaSuccess)) {
     faces_destroy(c);
     return cuda_fail(e, "faces_create: device allocation");
@@ -234,6 +246,7 @@ int faces_destroy(faces_ctx *c)
   cudaFree(c->d_roff);
   cudaFree(c->d_msg);
   cudaFree(c->d_scratch);
+  cudaFree(c->d_sync);
   cudaFree(c->d_field);
   cudaFree(c->d_field2);
   for (cudaStream_t st : {c->s_up, c->s_down})
@@ -303,12 +316,24 @@ int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *bloc
   return FACES_OK;
 }
 
+int faces_status(faces_ctx *c, int *bits)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (!bits) return fail(FACES_EINVAL, "null output pointer");
+  int v[2] = {0, 0};
+  CUDA_TRY(cudaMemcpy(v, c->d_sync + 1, sizeof(v), cudaMemcpyDeviceToHost), "status: read");
+  CUDA_TRY(cudaMemset(c->d_sync + 1, 0, sizeof(unsigned long long)), "status: clear");
+  *bits = v[0];
+  return FACES_OK;
+}
+
 int faces_launches_per_share(const faces_ctx *c, int compute)
 {
   if (int rc = check_ctx(c)) return rc;
   if (c->flags & FACES_V6) return 6;
   if (c->flags & FACES_V6F) return 4;
   if (compute && seam_step(*c) && c->splan.lean && c->splan.plane_items > 0) return 2;
+  if (pack_in_tiles(*c, compute)) return 1;
   return (c->flags & FACES_MESSAGES) ? 2 : 1;
 }
 
@@ -323,16 +348,24 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
     CUDA_TRY(launch_v6_fused(f, c->d_msg, compute, s), "fused v-6 kernel launch");
     return FACES_OK;
   }
-  if (c->flags & FACES_MESSAGES) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   const bool fused = compute && !(c->flags & FACES_GATHER);
+  const bool pack_fused = pack_in_tiles(*c, compute);
+  if ((c->flags & FACES_MESSAGES) && !pack_fused) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   if (fused && seam_step(*c)) {
     CUDA_TRY(launch_seams(f, c->splan, s), "seam kernel launch");
     return FACES_OK;
   }
   if (fused && !(c->flags & FACES_ROWS) && c->variant != 2 && tile_kernel_supported(c->n)) {
     const bool general = (c->flags & FACES_GENERAL) || c->variant == 1;
-    if (c->tplan.order == 3 && !general) CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
-    else CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general), "tile kernel launch");
+    if (c->tplan.order == 3 && !general) {
+      CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
+    } else if (pack_fused) {
+      const PackGrid g = pack_grid(f);
+      const PackFuse pf{g.gx, g.gy, g.wide ? 1 : 0, c->d_sync, reinterpret_cast<int *>(c->d_sync + 1)};
+      CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general, &pf), "message-mode tile kernel launch");
+    } else {
+      CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general), "tile kernel launch");
+    }
   } else if (fused && row_kernel_supported(c->n))
     CUDA_TRY(launch_rows(f, c->plan, s), "row kernel launch");
   else

@@ -30,6 +30,7 @@
 
 #include "geom.cuh"
 #include "kernels.cuh"
+#include "pack_steps.cuh"
 #include "rows_setup.cuh"
 #include "seam_steps.cuh"
 #include "v6_steps.cuh"
@@ -108,75 +109,12 @@ __global__ void init_int_kernel(FieldDesc f, long slabs, unsigned long long seed
 // pack: the 26 messages of every rank, raw values before any sum
 // ---------------------------------------------------------------------------
 
-// Directions in launch order: the six faces, then the twelve edges and the
-// eight corners.
-__constant__ int kPackDirs[26] = {4,  10, 12, 14, 16, 22, 1,  3,  5,  7,  9,  11, 15,
-                                  17, 19, 21, 23, 25, 0,  2,  6,  8,  18, 20, 24, 26};
-
-// Block rows 0 .. nranks*6-1: one face message each (rank, face), the row's
-// blocks striding over it.  Blocks beyond: one edge or corner message each
-// (nranks*20 of them, numbered across the remaining rows).  The free axes'
-// coordinates come from I-typed (32-bit where the message allows) divisions,
-// and the source offset from per-axis strides set up once per block, so the
-// per-point work is two or three divisions and one load.
+// pack_block (pack_steps.cuh): one block of the pack, also the fused
+// message-mode tile kernel's prologue
 template <typename I>
 __global__ void pack_kernel(FieldDesc f)
 {
-  const int face_rows = f.nranks * 6;
-  int r, dir;
-  I part, parts;
-  if ((int)blockIdx.y < face_rows) {
-    r = blockIdx.y / 6;
-    dir = kPackDirs[blockIdx.y % 6];
-    part = blockIdx.x;
-    parts = gridDim.x;
-  } else {
-    const int e = ((int)blockIdx.y - face_rows) * (int)gridDim.x + (int)blockIdx.x;
-    if (e >= f.nranks * 20) return;
-    r = e / 20;
-    dir = kPackDirs[6 + e % 20];
-    part = 0;
-    parts = 1;
-  }
-  const int rd = r * 27 + dir;
-  if (f.msg_off[rd] < 0) return;
-  const int d[3] = {dir % 3 - 1, (dir / 3) % 3 - 1, dir / 9 - 1};
-  const long n = f.n;
-  // fixed axes: the boundary row of the boundary element; free axes in
-  // ascending order, the message's i-then-j position order (region_pos).
-  // Scalars, not arrays indexed by axis, so that nothing goes to local memory.
-  long base = (long)r * f.R, si0 = 0, sj0 = 0, si1 = 0, sj1 = 0;
-  int nfree = 0, m0 = 1;
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const long sia = a == 0 ? 1 : a == 1 ? n : n * n;
-    const long sja = a == 0 ? n * n * n : a == 1 ? f.sjy : f.sjz;
-    if (d[a] == 0) {
-      if (nfree == 0) { si0 = sia; sj0 = sja; m0 = f.m[a]; }
-      else { si1 = sia; sj1 = sja; }
-      nfree++;
-    } else if (d[a] > 0) {
-      base += (n - 1) * sia + (long)(f.m[a] - 1) * sja;
-    }
-  }
-  const I sz = (I)region_size(f, d);
-  double *out = f.msg + f.msg_off[rd];
-  const double *ur = f.u + base;
-  const I nn = (I)(nfree == 2 ? n * n : n), nI = (I)n, mI = (I)m0;
-  for (I pos = part * (I)blockDim.x + threadIdx.x; pos < sz; pos += parts * (I)blockDim.x) {
-    long src;
-    if (nfree == 0) {
-      src = 0;
-    } else {
-      const I q = pos % nn, e = pos / nn;
-      if (nfree == 1) {
-        src = (long)q * si0 + (long)e * sj0;
-      } else {
-        src = (long)(q % nI) * si0 + (long)(q / nI) * si1 + (long)(e % mI) * sj0 + (long)(e / mI) * sj1;
-      }
-    }
-    out[pos] = ur[src];
-  }
+  pack_block<I>(f, (int)blockIdx.y, (int)blockIdx.x, (int)gridDim.x, (int)threadIdx.x, (int)blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -682,22 +620,9 @@ cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaSt
 
 cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)
 {
-  // face rows strided by about two waves of 8 blocks per SM, then one block
-  // per edge or corner message, in one launch
-  const int dface[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-  const int dedge[3][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}};
-  long face = 0, edge = 1;
-  for (int a = 0; a < 3; a++) {
-    face = face > region_size(f, dface[a]) ? face : region_size(f, dface[a]);
-    edge = edge > region_size(f, dedge[a]) ? edge : region_size(f, dedge[a]);
-  }
-  const long face_rows = (long)f.nranks * 6, small = (long)f.nranks * 20;
-  long bx = (face + 255) / 256;
-  const long want = (152L * 8 * 2 + face_rows - 1) / face_rows;
-  if (bx > want) bx = want;
-  if (bx < 1) bx = 1;
-  const dim3 grid((unsigned)bx, (unsigned)(face_rows + (small + bx - 1) / bx));
-  if (face + 256L * bx < (1L << 31) && edge < (1L << 30)) pack_kernel<unsigned><<<grid, 256, 0, s>>>(f);
+  const PackGrid g = pack_grid(f);
+  const dim3 grid((unsigned)g.gx, (unsigned)g.gy);
+  if (!g.wide) pack_kernel<unsigned><<<grid, 256, 0, s>>>(f);
   else pack_kernel<unsigned long><<<grid, 256, 0, s>>>(f);
   return cudaGetLastError();
 }

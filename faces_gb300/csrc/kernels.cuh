@@ -58,7 +58,19 @@ cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaS
 
 // periodic direct-mode fields take the periodic tile step, other fields the
 // mixed step (periodic step on interior tiles), unless `general`
-cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false);
+// The pack fused into the message-mode tile kernel's prologue: every block
+// packs its share of the pack's blocks (pack_steps.cuh, grid gx x gy), then
+// adds one to *counter; a tile that reads a message or writes a point the
+// pack reads first waits (bounded) until all blocks have; a wait that runs
+// out sets bit 0 of *err.  The launch is cooperative (all blocks resident)
+// and zeroes *counter before it.
+struct PackFuse {
+  int gx, gy, wide;
+  unsigned long long *counter;
+  int *err;
+};
+cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false,
+                         const PackFuse *fuse = nullptr);
 
 // Closed-form check of a field after `nshares` shares of a known initial
 // state (init: 0 = reference formula, 1 = integer seed) with the relative

@@ -97,20 +97,21 @@ cudaError_t launch_wtiles(const FieldDesc &f, const RowPlan &p, long grid, cudaS
   }
 }
 
-cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general)
+cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general,
+                         const PackFuse *fuse)
 {
   switch (f.n) {
-    case 2: return tiles_n2(f, p, grid, general, s);
-    case 3: return tiles_n3(f, p, grid, general, s);
-    case 4: return tiles_n4(f, p, grid, general, s);
-    case 5: return tiles_n5(f, p, grid, general, s);
-    case 6: return tiles_n6(f, p, grid, general, s);
-    case 7: return tiles_n7(f, p, grid, general, s);
-    case 8: return tiles_n8(f, p, grid, general, s);
-    case 9: return tiles_n9(f, p, grid, general, s);
-    case 10: return tiles_n10(f, p, grid, general, s);
-    case 11: return tiles_n11(f, p, grid, general, s);
-    case 12: return tiles_n12(f, p, grid, general, s);
+    case 2: return tiles_n2(f, p, grid, general, s, fuse);
+    case 3: return tiles_n3(f, p, grid, general, s, fuse);
+    case 4: return tiles_n4(f, p, grid, general, s, fuse);
+    case 5: return tiles_n5(f, p, grid, general, s, fuse);
+    case 6: return tiles_n6(f, p, grid, general, s, fuse);
+    case 7: return tiles_n7(f, p, grid, general, s, fuse);
+    case 8: return tiles_n8(f, p, grid, general, s, fuse);
+    case 9: return tiles_n9(f, p, grid, general, s, fuse);
+    case 10: return tiles_n10(f, p, grid, general, s, fuse);
+    case 11: return tiles_n11(f, p, grid, general, s, fuse);
+    case 12: return tiles_n12(f, p, grid, general, s, fuse);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -7,22 +7,34 @@
 #include <atomic>
 
 #include "geom.cuh"
+#include "kernels.cuh"
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
 
 namespace faces {
 
-cudaError_t tiles_n2(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n3(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n4(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n5(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n6(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n7(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n8(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n9(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n10(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n11(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
-cudaError_t tiles_n12(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s);
+cudaError_t tiles_n2(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n3(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n4(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n5(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n6(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n7(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n8(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n9(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n10(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n11(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
+cudaError_t tiles_n12(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse);
 
 cudaError_t wtiles_n2(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);
 cudaError_t wtiles_n3(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s);

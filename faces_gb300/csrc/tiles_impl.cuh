@@ -14,6 +14,7 @@
 
 #include "geom.cuh"
 #include "kernels.cuh"
+#include "pack_steps.cuh"
 #include "ptile_steps.cuh"
 #include "rows_setup.cuh"
 #include "tile_ops.cuh"
@@ -145,8 +146,33 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
 // only the rank's own copies stored.  Tile i is described (addresses, from
 // the receive table) in iteration i-3, staged in iteration i-2 and summed in
 // iteration i: NS data stages and NS+1 records, two block barriers per tile.
-template <int N, int K, int NS, bool OPEN>
-__global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
+// The fused pack's wait: thread 0 of a block polls the arrival counter
+// (acquire loads, short sleeps) until every block of the launch has packed,
+// at most kPackWaitPolls times; a wait that runs out sets bit 0 of *err and
+// lets the block go on (its results are then not to be trusted: the host
+// reads the flag with faces_status).
+constexpr long kPackWaitPolls = 1L << 22;
+
+__device__ __forceinline__ unsigned long long pack_arrivals(const unsigned long long *counter)
+{
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(counter) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void pack_wait(const PackFuse &pf, unsigned long long blocks)
+{
+  for (long i = 0; pack_arrivals(pf.counter) < blocks; i++) {
+    if (i == kPackWaitPolls) {
+      atomicOr(pf.err, 1);
+      return;
+    }
+    __nanosleep(64);
+  }
+}
+
+template <int N, int K, int NS, bool OPEN, bool FUSE>
+__global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p, PackFuse pf)
 {
   constexpr int stage = tile_stage_size<N, K>();
   constexpr int NR = NS + 1;
@@ -155,6 +181,33 @@ __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
   static_assert(sizeof(XMeta) % 16 == 0, "tile records keep 16-byte alignment");
   XMeta *rec = reinterpret_cast<XMeta *>(sm + NS * stage);
   const int t = threadIdx.x;
+  if constexpr (FUSE) {
+    // the pack: this block's share of its blocks, then its arrival (every
+    // block arrives once, whether or not it has tiles)
+    const long pb = (long)pf.gx * pf.gy;
+    for (long v = blockIdx.x; v < pb; v += gridDim.x) {
+      const int vx = (int)(v % pf.gx), vy = (int)(v / pf.gx);
+      if (pf.wide) pack_block<unsigned long>(f, vy, vx, pf.gx, t, 256);
+      else pack_block<unsigned>(f, vy, vx, pf.gx, t, 256);
+    }
+    __syncthreads();
+    if (t == 0) {
+      __threadfence();
+      atomicAdd(pf.counter, 1ULL);
+    }
+  }
+  // Before a tile that reads a message or writes a boundary point is
+  // staged, every block must have packed (block-uniform: the record is in
+  // shared memory); interior tiles run beside other blocks' packing.
+  bool packed = !FUSE;
+  auto ready = [&](const XMeta *r) {
+    if (FUSE && !packed && !xtile::interior(r)) {
+      if (t == 0) pack_wait(pf, gridDim.x);
+      __syncthreads();
+      (void)pack_arrivals(pf.counter);  // every thread's own acquire
+      packed = true;
+    }
+  };
   TileWalk nw;
   walk_begin(p, nw);
   if (nw.done) return;
@@ -167,16 +220,24 @@ __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p)
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < NS - 1; j++) {
-    if (j < ndesc) xtile::xcopies<N, K, OPEN>(rec + j, sm + j * stage, t);
-    else cp_commit();
+    if (j < ndesc) {
+      ready(rec + j);
+      xtile::xcopies<N, K, OPEN>(rec + j, sm + j * stage, t);
+    } else {
+      cp_commit();
+    }
   }
   for (int i = 0; i < ndesc; i++) {
     cp_wait<NS - 2>();
     // tile i's stage, the records up to i+NS-1, and the end of tile i-1's
     // stores (its stage and record are free again)
     __syncthreads();
-    if (i + NS - 1 < ndesc) xtile::xcopies<N, K, OPEN>(rec + (i + NS - 1) % NR, sm + ((i + NS - 1) % NS) * stage, t);
-    else cp_commit();
+    if (i + NS - 1 < ndesc) {
+      ready(rec + (i + NS - 1) % NR);
+      xtile::xcopies<N, K, OPEN>(rec + (i + NS - 1) % NR, sm + ((i + NS - 1) % NS) * stage, t);
+    } else {
+      cp_commit();
+    }
     double *buf = sm + (i % NS) * stage;
     const XMeta *r = rec + i % NR;
     // an open field's tiles away from its boundary are complete: they take
@@ -342,24 +403,58 @@ inline cudaError_t launch_wtiles_n(const FieldDesc &f, const RowPlan &p, long gr
   return cudaGetLastError();
 }
 
+// The message-mode step with the pack in its prologue: one cooperative
+// launch (every block resident, so that a block's wait for the others ends),
+// the grid capped at what is resident, the arrival counter zeroed first.
+template <int N, int K, bool OPEN>
+inline cudaError_t launch_xtile_fused(const FieldDesc &f, const RowPlan &p, long grid, size_t smem,
+                                      const PackFuse &pf, cudaStream_t s)
+{
+  const void *kern = (const void *)xtile_kernel<N, K, kTileStages, OPEN, true>;
+  static std::atomic<unsigned long long> configured{0};
+  if (cudaError_t e = raise_smem_limit(kern, (int)smem, configured)) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem)) != cudaSuccess)
+    return e;
+  if (grid > (long)per_sm * sms) grid = (long)per_sm * sms;
+  if (grid < 1) return cudaErrorCooperativeLaunchTooLarge;
+  if ((e = cudaMemsetAsync(pf.counter, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
+  FieldDesc fa = f;
+  RowPlan pa = p;
+  PackFuse pfa = pf;
+  void *args[] = {&fa, &pa, &pfa};
+  return cudaLaunchCooperativeKernel(kern, dim3((unsigned)grid), dim3(256), args, smem, s);
+}
+
 template <int N, int K>
-inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                                   const PackFuse *fuse)
 {
   static_assert(tile_stage_size<N, K>() * sizeof(double) % 16 == 0, "stage alignment");
   if (grid > p.ntiles) grid = p.ntiles;
   if (grid < 1) return cudaSuccess;
   if (!general && xtile_field(f)) {
     const size_t smem = sizeof(double) * kTileStages * tile_stage_size<N, K>() + sizeof(XMeta) * (kTileStages + 1);
+    if (fuse && f.mode == kMessages) {
+      if (f.periodic) return launch_xtile_fused<N, K, false>(f, p, grid, smem, *fuse, s);
+      return launch_xtile_fused<N, K, true>(f, p, grid, smem, *fuse, s);
+    }
+    const PackFuse none{};
     if (f.periodic) {
       static std::atomic<unsigned long long> configured{0};
-      if (cudaError_t e = raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, false>, (int)smem, configured))
+      if (cudaError_t e =
+              raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, false, false>, (int)smem, configured))
         return e;
-      xtile_kernel<N, K, kTileStages, false><<<(unsigned)grid, 256, smem, s>>>(f, p);
+      xtile_kernel<N, K, kTileStages, false, false><<<(unsigned)grid, 256, smem, s>>>(f, p, none);
     } else {
       static std::atomic<unsigned long long> configured{0};
-      if (cudaError_t e = raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, true>, (int)smem, configured))
+      if (cudaError_t e =
+              raise_smem_limit((const void *)xtile_kernel<N, K, kTileStages, true, false>, (int)smem, configured))
         return e;
-      xtile_kernel<N, K, kTileStages, true><<<(unsigned)grid, 256, smem, s>>>(f, p);
+      xtile_kernel<N, K, kTileStages, true, false><<<(unsigned)grid, 256, smem, s>>>(f, p, none);
     }
   } else if (!general && !ptile_field(f)) {
     const size_t smem = tile_smem_bytes(N, K) + sizeof(PMeta) * kTileStages;
@@ -382,20 +477,21 @@ inline cudaError_t launch_tiles_nk(const FieldDesc &f, const RowPlan &p, long gr
 }
 
 template <int N>
-inline cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+inline cudaError_t launch_tiles_n(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                                  const PackFuse *fuse)
 {
   constexpr int KM = tile_kinst_max(N);
   if (p.chunk > KM) return cudaErrorInvalidValue;
   switch (tile_instance_k(p.chunk)) {
-    case 1: return launch_tiles_nk<N, 1>(f, p, grid, general, s);
-    case 2: return launch_tiles_nk<N, 2>(f, p, grid, general, s);
-    case 4: return launch_tiles_nk<N, 4>(f, p, grid, general, s);
-    case 8: return launch_tiles_nk<N, 8>(f, p, grid, general, s);
+    case 1: return launch_tiles_nk<N, 1>(f, p, grid, general, s, fuse);
+    case 2: return launch_tiles_nk<N, 2>(f, p, grid, general, s, fuse);
+    case 4: return launch_tiles_nk<N, 4>(f, p, grid, general, s, fuse);
+    case 8: return launch_tiles_nk<N, 8>(f, p, grid, general, s, fuse);
     case 16:
-      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, general, s);
+      if constexpr (KM >= 16) return launch_tiles_nk<N, 16>(f, p, grid, general, s, fuse);
       return cudaErrorInvalidValue;
     case 32:
-      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, general, s);
+      if constexpr (KM >= 32) return launch_tiles_nk<N, 32>(f, p, grid, general, s, fuse);
       return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }

@@ -3,9 +3,10 @@
 
 namespace faces {
 
-cudaError_t tiles_n10(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s)
+cudaError_t tiles_n10(const FieldDesc &f, const RowPlan &p, long grid, bool general, cudaStream_t s,
+                     const PackFuse *fuse)
 {
-  return launch_tiles_n<10>(f, p, grid, general, s);
+  return launch_tiles_n<10>(f, p, grid, general, s, fuse);
 }
 
 cudaError_t wtiles_n10(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s)

@@ -257,6 +257,14 @@ __host__ __device__ __forceinline__ void xdescribe(const FieldDesc &f, const Row
   }
 }
 
+// A tile that reads no message and writes no point of the rank's boundary
+// (what the pack reads): its four columns and their lower ends are the
+// rank's own (not a first chunk), and it is not its column's last chunk.
+__host__ __device__ __forceinline__ bool interior(const XMeta *rec)
+{
+  return rec->wcol == 15 && rec->wlo == 15 && !(rec->flags & 1);
+}
+
 // presence bits of a described tile's columns and lower ends (all, in a
 // periodic field)
 template <bool OPEN>

@@ -79,6 +79,18 @@ extern "C" {
                                kernel is still the default for direct-mode
                                fields with n >= 11 (FACES_ROWS and
                                FACES_GENERAL keep theirs). */
+#define FACES_PACK_FUSED 0x100u /* message mode: the pack in the tile
+                               kernel's prologue, one cooperative launch
+                               per share (FUSE_SEND/FUSE_INNER of gpu/v-26-
+                               messages/Faces.cc:175-239,301-343 on one
+                               device): each block packs its share of the
+                               pack's blocks, tiles that read a message or
+                               write a subdomain-boundary point wait until
+                               every block has, interior tiles run beside
+                               the packing.  Same results; measured about
+                               2% slower than the default (the pack as its
+                               own launch, then the tile step) on a 3x3x3
+                               grid of 16^3 n=6 ranks. */
 
 typedef struct faces_ctx faces_ctx;
 
@@ -185,6 +197,12 @@ int faces_autotune(faces_ctx *ctx, double *u, int compute, int trials, void *str
  * faces_set_tuning; 3 warp tiles; seam kernel: 0 chunked, 1 lean).  Any
  * pointer may be NULL. */
 int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *blocks, int *kernel, int *order);
+
+/* The device-side status bits of the fused message-mode step
+ * (FACES_PACK_FUSED), read and cleared (synchronous): bit 0 = a block's wait
+ * for the others' packing ran out (bounded, about a second; the shares since
+ * the last call are then not to be trusted).  0 when all is well. */
+int faces_status(faces_ctx *ctx, int *bits);
 
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);

@@ -41,6 +41,7 @@
 #include "rows_setup.cuh"
 #include "tables.h"
 #include "tile_ops.cuh"
+#include "pack_steps.cuh"
 #include "xtile_steps.cuh"
 
 using namespace faces;
@@ -270,7 +271,7 @@ void host_pack(const FieldDesc &f, const double *u, double *msg, const std::vect
 
 template <int N, int K, int T, bool OPEN>
 int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, long msg_total, const RowPlan &p,
-            Err &e)
+            const std::vector<char> &packread, Err &e)
 {
   constexpr int stage = tile_stage_size<N, K>();
   const long ncol = p.ntiles / p.nchunks;
@@ -331,11 +332,19 @@ int xreplay(FieldDesc f, double *live, double *snap, long total, double *msg, lo
     }
     written_once(before, live, total, e, tile);
     if (!guards_intact(sm, stage)) e.set("stage guard cells changed", tile);
+    // the fused pack: an interior tile runs beside the other blocks' packing,
+    // so it may change no point the pack reads (its record holds no message:
+    // every address in it is marked own, checked above)
+    if (!packread.empty() && xtile::interior(&meta))
+      for (long i = 0; i < total && e.ok; i++)
+        if (packread[i] && std::memcmp(&before[i], live + i, sizeof(double)) != 0)
+          e.set("an interior tile changed a point the pack reads", tile);
   }
   return e.ok ? 0 : -1;
 }
 
-using XReplayFn = int (*)(FieldDesc, double *, double *, long, double *, long, const RowPlan &, Err &);
+using XReplayFn = int (*)(FieldDesc, double *, double *, long, double *, long, const RowPlan &,
+                          const std::vector<char> &, Err &);
 
 template <int N, int K>
 XReplayFn xpick_t(int T, bool open)
@@ -427,9 +436,33 @@ extern "C" int xtile_emulate(int lx, int ly, int lz, int mx, int my, int mz, int
     std::memcpy(snap.data() + kGuard, u, sizeof(double) * total);
     std::fill(msg.begin() + kGuard, msg.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
     host_pack(f, u, msg.data() + kGuard, off);
+    // the device pack (pack_steps.cuh, the fused kernel's prologue) on every
+    // block of its grid: the same messages, and the points it reads
+    std::vector<char> packread;
+    if (messages) {
+      packread.assign(total, 0);
+      std::vector<double> msg2(msg_total, std::numeric_limits<double>::quiet_NaN());
+      FieldDesc fp = f;
+      fp.u = u;
+      fp.msg = msg2.data();
+      const PackGrid g = pack_grid(fp);
+      auto touch = [&](const double *q) {
+        const long i = (long)(q - u);
+        if (i < 0 || i >= total) e.set("the pack reads outside the field", -1);
+        else packread[i] = 1;
+      };
+      for (int by = 0; by < g.gy && e.ok; by++)
+        for (int bx = 0; bx < g.gx; bx++)
+          for (int t = 0; t < 256; t++) {
+            if (g.wide) pack_block<unsigned long>(fp, by, bx, g.gx, t, 256, touch);
+            else pack_block<unsigned>(fp, by, bx, g.gx, t, 256, touch);
+          }
+      if (e.ok && std::memcmp(msg2.data(), msg.data() + kGuard, sizeof(double) * msg_total) != 0)
+        e.set("the device pack's messages differ from the host pack's", -1);
+    }
     msg_copy = msg;
     std::fill(live.begin() + kGuard, live.end() - kGuard, std::numeric_limits<double>::quiet_NaN());
-    fn(f, live.data() + kGuard, snap.data() + kGuard, total, msg.data() + kGuard, msg_total, p, e);
+    fn(f, live.data() + kGuard, snap.data() + kGuard, total, msg.data() + kGuard, msg_total, p, packread, e);
     if (e.ok && (!guards_intact(live, total) || !guards_intact(snap, total))) e.set("field guard cells changed", -1);
     if (e.ok && tiledev::host_misaligned_copies() != 0) e.set("a 16-byte copy from or to an address not 16-byte aligned", -1);
     if (e.ok && std::memcmp(msg.data(), msg_copy.data(), sizeof(double) * msg.size()) != 0)

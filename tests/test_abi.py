@@ -41,7 +41,7 @@ def test_argument_errors_without_gpu(faces_lib):
     L = F.lib()
     h = ctypes.c_void_p()
     for args in [(1, 1, 1, 4, 4, 4, 1, 0), (0, 1, 1, 4, 4, 4, 5, 0), (1, 1, 1, 4, 0, 4, 5, 0),
-                 (1, 1, 1, 4, 4, 4, 5, 0x100), (1, 1, 1, 4, 4, 4, 5, 0x80 | 0x2)]:
+                 (1, 1, 1, 4, 4, 4, 5, 0x200), (1, 1, 1, 4, 4, 4, 5, 0x80 | 0x2)]:
         assert L.faces_create(ctypes.byref(h), *args) == -1
         assert L.faces_last_error()
     assert L.faces_share(None, None, 1, None) == -1

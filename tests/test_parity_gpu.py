@@ -318,3 +318,31 @@ def test_run_host_many(oracle, faces_lib, messages):
     with pytest.raises(F.FacesError):
         f.run_host_many([ins[0], outs[0]], [outs[0], outs[1]], 3)
     f.close()
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 3, 4, 3, 2, 6), (2, 1, 2, 5, 3, 4, 5), (3, 3, 3, 16, 16, 16, 6),
+                                   (2, 2, 1, 9, 7, 5, 11), (1, 1, 1, 6, 5, 4, 8)],
+                         ids=lambda s: "x".join(map(str, s)))
+@pytest.mark.parametrize("periodic", [False, True], ids=["open", "periodic"])
+def test_fused_pack_equals_separate(oracle, faces_lib, shape, periodic):
+    """v-26 message mode with the pack in the tile kernel's prologue
+    (FACES_PACK_FUSED: one cooperative launch per share) and as its own
+    launch (the default): the same bits, the oracle's, and no wait of the
+    fused form ran out."""
+    O, F = oracle, faces_lib
+    outs = []
+    for sep in (False, True):
+        f = F.Faces(*shape, periodic=periodic, messages=True, pack_fused=not sep)
+        assert f.launches_per_share() == (2 if sep else 1)
+        u = f.field()
+        f.init_int(u, 3)
+        f.share_n(u, 4)
+        chk = f.check(u, init="int", seed=3, nshares=4)
+        assert chk.passed and chk.maxrel == 0.0, (sep, chk)
+        assert f.status() == 0
+        outs.append(u)
+        f.close()
+    assert torch.equal(outs[0], outs[1])
+    s = O.Shape(*shape, periodic=periodic)
+    if s.total_doubles < 20_000_000:
+        assert np.array_equal(outs[0].cpu().numpy(), O.groups_share(s, O.init_int(s, 3), True, 4))
