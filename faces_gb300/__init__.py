@@ -74,6 +74,7 @@ def lib() -> ctypes.CDLL:
     L.faces_set_tuning.argtypes = [vp, c_int, c_int, c_int]
     L.faces_launches_per_share.argtypes = [vp, c_int]
     L.faces_status.argtypes = [vp, ctypes.POINTER(c_int)]
+    L.faces_test_pack_wait.argtypes = [vp, c_int, c_long]
     L.faces_autotune.argtypes = [vp, dp, c_int, c_int, vp]
     L.faces_autotune.restype = c_int
     L.faces_get_tuning.argtypes = [vp] + [ctypes.POINTER(c_int)] * 5
@@ -353,6 +354,11 @@ class Faces:
 
     def launches_per_share(self, compute: bool = True) -> int:
         return _check(lib().faces_launches_per_share(self._h, int(compute)))
+
+    def test_pack_wait(self, extra: int, polls: int = 1 << 22) -> None:
+        """Test hook: the fused step's waits expect `extra` (0 or 1) more
+        arrivals than exist, so that they run out after `polls` polls."""
+        _check(lib().faces_test_pack_wait(self._h, extra, polls))
 
     def status(self) -> int:
         """Device status bits, read and cleared (synchronous): bit 0 = the

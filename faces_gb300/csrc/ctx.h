@@ -26,6 +26,8 @@ struct faces_ctx {
   double *d_msg = nullptr;
   unsigned long long *d_scratch = nullptr;  // check: rank maxima, max, first, values
   unsigned long long *d_sync = nullptr;     // fused pack: [0] arrivals, [1] the wait's error bits
+  int pack_wait_extra = 0;                  // test hook (faces_test_pack_wait)
+  long pack_wait_polls = 1L << 22;          // the fused pack's wait bound (about a second)
   double *d_field = nullptr;                // faces_run_host's device copy
   // faces_run_host_many: a second device field, copy streams and the events
   // that order uploads, shares and downloads of the two fields

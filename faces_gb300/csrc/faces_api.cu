@@ -316,6 +316,15 @@ int faces_get_tuning(const faces_ctx *c, int *chunk, int *unit_chunks, int *bloc
   return FACES_OK;
 }
 
+int faces_test_pack_wait(faces_ctx *c, int extra, long polls)
+{
+  if (int rc = check_ctx(c)) return rc;
+  if (extra < 0 || extra > 1 || polls < 1) return fail(FACES_EINVAL, "extra %d (0 or 1), polls %ld (>= 1)", extra, polls);
+  c->pack_wait_extra = extra;
+  c->pack_wait_polls = polls;
+  return FACES_OK;
+}
+
 int faces_status(faces_ctx *c, int *bits)
 {
   if (int rc = check_ctx(c)) return rc;
@@ -361,7 +370,8 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
       CUDA_TRY(launch_wtiles(f, c->tplan, c->tgrid, s), "warp tile kernel launch");
     } else if (pack_fused) {
       const PackGrid g = pack_grid(f);
-      const PackFuse pf{g.gx, g.gy, g.wide ? 1 : 0, c->d_sync, reinterpret_cast<int *>(c->d_sync + 1)};
+      const PackFuse pf{g.gx,    g.gy, g.wide ? 1 : 0, c->d_sync, reinterpret_cast<int *>(c->d_sync + 1),
+                        c->pack_wait_extra, c->pack_wait_polls};
       CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general, &pf), "message-mode tile kernel launch");
     } else {
       CUDA_TRY(launch_tiles(f, c->tplan, c->tgrid, s, general), "tile kernel launch");

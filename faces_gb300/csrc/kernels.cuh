@@ -68,6 +68,8 @@ struct PackFuse {
   int gx, gy, wide;
   unsigned long long *counter;
   int *err;
+  int extra;   // arrivals waited for beyond the launch's blocks (0; a test sets 1)
+  long polls;  // the wait's bound (polls of about 64 ns or more)
 };
 cudaError_t launch_tiles(const FieldDesc &f, const RowPlan &p, long grid, cudaStream_t s, bool general = false,
                          const PackFuse *fuse = nullptr);

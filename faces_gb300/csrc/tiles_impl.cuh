@@ -148,10 +148,9 @@ __global__ void __launch_bounds__(256, 4) ptile_kernel(FieldDesc f, RowPlan p)
 // iteration i: NS data stages and NS+1 records, two block barriers per tile.
 // The fused pack's wait: thread 0 of a block polls the arrival counter
 // (acquire loads, short sleeps) until every block of the launch has packed,
-// at most kPackWaitPolls times; a wait that runs out sets bit 0 of *err and
-// lets the block go on (its results are then not to be trusted: the host
-// reads the flag with faces_status).
-constexpr long kPackWaitPolls = 1L << 22;
+// at most pf.polls times; a wait that runs out sets bit 0 of *err and lets
+// the block go on (its results are then not to be trusted: the host reads the
+// flag with faces_status).
 
 __device__ __forceinline__ unsigned long long pack_arrivals(const unsigned long long *counter)
 {
@@ -163,7 +162,7 @@ __device__ __forceinline__ unsigned long long pack_arrivals(const unsigned long 
 __device__ __forceinline__ void pack_wait(const PackFuse &pf, unsigned long long blocks)
 {
   for (long i = 0; pack_arrivals(pf.counter) < blocks; i++) {
-    if (i == kPackWaitPolls) {
+    if (i >= pf.polls) {
       atomicOr(pf.err, 1);
       return;
     }
@@ -202,7 +201,7 @@ __global__ void __launch_bounds__(256, 4) xtile_kernel(FieldDesc f, RowPlan p, P
   bool packed = !FUSE;
   auto ready = [&](const XMeta *r) {
     if (FUSE && !packed && !xtile::interior(r)) {
-      if (t == 0) pack_wait(pf, gridDim.x);
+      if (t == 0) pack_wait(pf, gridDim.x + (unsigned)pf.extra);
       __syncthreads();
       (void)pack_arrivals(pf.counter);  // every thread's own acquire
       packed = true;

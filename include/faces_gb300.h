@@ -204,6 +204,14 @@ int faces_get_tuning(const faces_ctx *ctx, int *chunk, int *unit_chunks, int *bl
  * the last call are then not to be trusted).  0 when all is well. */
 int faces_status(faces_ctx *ctx, int *bits);
 
+/* Test hook for the fused step's bounded wait: with extra = 1 every block
+ * that waits waits for one more arrival than the launch has, so each such
+ * wait runs out after `polls` polls (of about 64 ns or more) and sets status
+ * bit 0 instead of hanging; extra = 0, polls = 4194304 are the defaults
+ * (about a second).  The shares run with extra = 1 are wrong; the context
+ * stays usable. */
+int faces_test_pack_wait(faces_ctx *ctx, int extra, long polls);
+
 /* Kernel launches one share enqueues with the current settings. */
 int faces_launches_per_share(const faces_ctx *ctx, int compute);
 

@@ -346,3 +346,29 @@ def test_fused_pack_equals_separate(oracle, faces_lib, shape, periodic):
     s = O.Shape(*shape, periodic=periodic)
     if s.total_doubles < 20_000_000:
         assert np.array_equal(outs[0].cpu().numpy(), O.groups_share(s, O.init_int(s, 3), True, 4))
+
+
+def test_fused_pack_wait_runs_out_and_reports(faces_lib):
+    """The fused step's wait is bounded: made to wait for an arrival that
+    never comes (test hook), every waiting block gives up after a short
+    bound, sets status bit 0 and returns; the status reads it once, and the
+    same context then shares correctly again."""
+    F = faces_lib
+    f = F.Faces(3, 3, 3, 4, 3, 2, 6, periodic=True, messages=True, pack_fused=True)
+    u = f.field()
+    f.init_int(u, 3)
+    f.share_n(u, 1)
+    torch.cuda.synchronize()
+    assert f.status() == 0
+    f.test_pack_wait(1, 1 << 12)
+    f.share_n(u, 1)
+    torch.cuda.synchronize()
+    assert f.status() == 1
+    assert f.status() == 0  # read and cleared
+    f.test_pack_wait(0)
+    f.init_int(u, 3)
+    f.share_n(u, 2)
+    chk = f.check(u, init="int", seed=3, nshares=2)
+    assert chk.passed and chk.maxrel == 0.0
+    assert f.status() == 0
+    f.close()
