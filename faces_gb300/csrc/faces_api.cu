@@ -131,6 +131,13 @@ void replan(faces_ctx &c)
     k = k2;
     // the form's shared memory at most 110 KB (two blocks per SM)
     while (k > 1 && tile_form_smem_bytes(c.n, k, form) > 110 * 1024) k /= 2;
+    // a default longer than the ~20 KB stage only where every block of two
+    // per SM still gets four tiles
+    if (c.chunk <= 0) {
+      const bool virt = (c.flags & FACES_MESSAGES) || !(c.flags & FACES_PERIODIC);
+      const long cols = (long)c.nranks * (c.m[1] + virt) * (c.m[2] + virt);
+      while (k > tile_kmax(c.n) && cols * ((c.m[0] + k - 1) / k) < 4L * 2 * c.sms) k /= 2;
+    }
     c.tplan = make_row_plan(f, k, 0);
     // order 3 (warp tiles) applies to the periodic step only; elsewhere it
     // means the default

@@ -17,14 +17,16 @@ bool tile_kernel_supported(int n) { return n >= 2 && n <= 12; }
 
 int tile_default_chunk(int n) { return tile_kmax(n); }
 
-// For n >= 10 the periodic and message-mode steps run faster with the
-// longest tile that still leaves two blocks per SM (at most 110 KB of
-// shared memory) than with ~20 KB stages: measured on 95x94x93 n = 12 (2
-// elements: 4.37 vs 4.84 ms per share periodic, 4.93 vs 5.34 open), 48^3
-// n = 10 (4 elements: 0.312 vs 0.337 ms) and 40^3 n = 11 (2: 0.276 vs 0.287).
+// The periodic and message-mode steps run faster with the longest tile that
+// still leaves two blocks per SM (at most 110 KB of shared memory) than with
+// ~20 KB stages: measured on 95x94x93 n = 12 (2 elements: 4.37 vs 4.84 ms per
+// share periodic, 4.93 vs 5.34 open), 48^3 n = 10 (4: 0.312 vs 0.337), 40^3
+// n = 11 (2: 0.276 vs 0.287), 48^3 n = 9 (4: 0.240 vs 0.261), 56^3 n = 7 (8:
+// 0.213 vs 0.278), 60^3 n = 5 (16: 0.112 vs 0.126); n = 6 and 8 keep their
+// lengths (8 and 4).  Small fields shorten it again (faces_api.cu).
 int tile_default_chunk(int n, TileForm form)
 {
-  if (form == kGeneralForm || n < 10) return tile_kmax(n);
+  if (form == kGeneralForm) return tile_kmax(n);
   int k = 1;
   while (k * 2 <= tile_kinst_max(n) && tile_form_smem_bytes(n, k * 2, form) <= 110 * 1024) k *= 2;
   return k;

@@ -59,11 +59,9 @@ def batch_warp_tile(n, stage=2688):
 
 def form_default_k(n, form):
     """the default tile length of the periodic ("p") and message-mode ("x")
-    steps: for n >= 10 the longest power of 2 whose three stages and tile
-    records stay within 110 KB (PMeta 80 B + int4 per stage; XMeta 240 B per
-    record, one more record than stages)"""
-    if n < 10:
-        return tile_kmax(n)
+    steps on a large field: the longest power of 2 (up to max(tile_kmax, 8))
+    whose three stages and tile records stay within 110 KB (PMeta 80 B +
+    int4 per stage; XMeta 240 B per record, one more record than stages)"""
     rec = 3 * 96 if form == "p" else 4 * 240
     k = 1
     while k * 2 <= max(tile_kmax(n), 8) and 8 * 3 * (2 * k * n * n * row_stride(n) + 2 * n * n) + rec <= 110 * 1024:
@@ -72,8 +70,8 @@ def form_default_k(n, form):
 
 
 def test_form_default_lengths():
-    assert [form_default_k(n, "p") for n in (10, 11, 12)] == [4, 2, 2]
-    assert [form_default_k(n, "x") for n in (10, 11, 12)] == [4, 2, 2]
+    assert [form_default_k(n, "p") for n in range(3, 13)] == [32, 16, 16, 8, 8, 4, 4, 4, 2, 2]
+    assert [form_default_k(n, "x") for n in range(3, 13)] == [32, 16, 16, 8, 8, 4, 4, 4, 2, 2]
 
 
 def tile_kwarp(n):
