@@ -29,11 +29,11 @@ struct faces_ctx {
   int pack_wait_extra = 0;                  // test hook (faces_test_pack_wait)
   long pack_wait_polls = 1L << 22;          // the fused pack's wait bound (about a second)
   double *d_field = nullptr;                // faces_run_host's device copy
-  // faces_run_host_many: a second device field, copy streams and the events
+  // faces_run_host_many: a second device field, its streams and the events
   // that order uploads, shares and downloads of the two fields
   double *d_field2 = nullptr;
   bool pipe_ready = false;
-  cudaStream_t s_up = nullptr, s_down = nullptr;
+  cudaStream_t s_up = nullptr, s_down = nullptr, s_comp = nullptr;  // uploads, downloads, shares
   cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int chunk = 0, tpb = 0, order = -1;
