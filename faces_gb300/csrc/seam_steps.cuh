@@ -140,9 +140,6 @@ FACES_HD void gather_point(const FieldDesc &f, int r, const int g[3], int comput
 // the seam step
 // ---------------------------------------------------------------------------
 
-// a field the seam step takes: direct mode (every copy in this memory)
-FACES_HD bool seam_field(const FieldDesc &f) { return f.mode == kDirect; }
-
 // slots per element: (a, b) in [0, n-1)^2, one point of each plane
 FACES_HD constexpr int seam_slots(int n) { return (n - 1) * (n - 1); }
 
