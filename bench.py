@@ -691,9 +691,10 @@ def run_reference(args) -> dict | None:
         "impl": "reference",
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's own code cannot run here (its GPU build needs its sources and MPI; "
-                "binaries built in the development container are x86): its v-26 loops, transcribed to C "
-                "with OpenMP, are timed instead",
+        "note": "the reference's CPU code for this operation is its Mugs checker (gpu/Mugs.cc), which has no "
+                "periodic neighbours, and this configuration is periodic: the reference's v-26 loops, transcribed "
+                "to C with OpenMP, are timed on it instead; the reference's own CUDA build runs beside this "
+                "repository's executable in the GPU arm's reference_gpu object",
     }
 
 
