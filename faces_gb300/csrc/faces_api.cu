@@ -75,12 +75,16 @@ int default_chunk(const faces_ctx &c)
   return (int)((c.m[0] + nch - 1) / nch);
 }
 
+// v-26 message mode on a field with no neighbour rank (one non-periodic
+// rank) has no message to pack or read: its share is the direct step's
+bool no_messages(const faces_ctx &c) { return (c.flags & FACES_MESSAGES) && c.msg_total == 0; }
+
 // the seam kernel runs this share: forced, the default, or chosen by
 // autotune (variant 3)
 bool seam_step(const faces_ctx &c)
 {
   return (c.variant == 3 || (c.flags & FACES_SEAMS)) && seam_kernel_supported(c.n) &&
-         !(c.flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F | FACES_GATHER));
+         !(c.flags & (FACES_V6 | FACES_V6F | FACES_GATHER)) && (!(c.flags & FACES_MESSAGES) || no_messages(c));
 }
 
 // message mode with FACES_PACK_FUSED: the pack runs in the message-mode
@@ -101,7 +105,8 @@ bool pack_in_tiles(const faces_ctx &c, int compute)
 int default_variant(const faces_ctx &c)
 {
   return c.n >= 11 && seam_kernel_supported(c.n) &&
-                 !(c.flags & (FACES_MESSAGES | FACES_V6 | FACES_V6F | FACES_GATHER | FACES_ROWS | FACES_GENERAL))
+                 !(c.flags & (FACES_V6 | FACES_V6F | FACES_GATHER | FACES_ROWS | FACES_GENERAL)) &&
+                 (!(c.flags & FACES_MESSAGES) || no_messages(c))
              ? 3
              : 0;
 }
@@ -350,7 +355,7 @@ int faces_launches_per_share(const faces_ctx *c, int compute)
   if (c->flags & FACES_V6F) return 4;
   if (compute && seam_step(*c) && c->splan.lean && c->splan.plane_items > 0) return 2;
   if (pack_in_tiles(*c, compute)) return 1;
-  return (c->flags & FACES_MESSAGES) ? 2 : 1;
+  return (c->flags & FACES_MESSAGES) && !no_messages(*c) ? 2 : 1;
 }
 
 static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
@@ -366,7 +371,7 @@ static int share_once(faces_ctx *c, double *u, int compute, cudaStream_t s)
   }
   const bool fused = compute && !(c->flags & FACES_GATHER);
   const bool pack_fused = pack_in_tiles(*c, compute);
-  if ((c->flags & FACES_MESSAGES) && !pack_fused) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
+  if ((c->flags & FACES_MESSAGES) && !pack_fused && !no_messages(*c)) CUDA_TRY(launch_pack(f, s), "pack kernel launch");
   if (fused && seam_step(*c)) {
     CUDA_TRY(launch_seams(f, c->splan, s), "seam kernel launch");
     return FACES_OK;
@@ -491,7 +496,7 @@ int faces_autotune(faces_ctx *c, double *u, int compute, int trials, void *strea
   // the seam kernel (direct mode): the chunked form (order 0) at its
   // default chunk (shortened for small fields) and at twice the unshortened
   // one, and the lean form (order 1)
-  if (!(c->flags & FACES_MESSAGES) && seam_kernel_supported(c->n)) {
+  if ((!(c->flags & FACES_MESSAGES) || no_messages(*c)) && seam_kernel_supported(c->n)) {
     const int e0 = seam_default_chunk(c->n);
     c->order = 0;
     for (int e : {0, 2 * e0}) {

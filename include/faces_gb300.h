@@ -46,7 +46,10 @@ extern "C" {
                                messages, the buffers are swapped by direction,
                                each rank unpack-adds its own copies.  Without
                                it one owner sums each shared point across
-                               ranks in place (same values, no messages). */
+                               ranks in place (same values, no messages).  A
+                               field with no neighbour rank (one non-periodic
+                               rank) has no message: it takes the direct
+                               step. */
 #define FACES_GATHER 0x4u   /* force the generic one-thread-per-point kernel */
 #define FACES_ROWS 0x8u     /* use the register row kernel instead of the
                                shared-memory tile kernel */

@@ -333,7 +333,9 @@ def test_fused_pack_equals_separate(oracle, faces_lib, shape, periodic):
     outs = []
     for sep in (False, True):
         f = F.Faces(*shape, periodic=periodic, messages=True, pack_fused=not sep)
-        assert f.launches_per_share() == (2 if sep else 1)
+        # one non-periodic rank has no message: no pack launch either way
+        alone = shape[0] * shape[1] * shape[2] == 1 and not periodic
+        assert f.launches_per_share() == (2 if sep and not alone else 1)
         u = f.field()
         f.init_int(u, 3)
         f.share_n(u, 4)
