@@ -190,7 +190,49 @@ FACES_HD void v6_sweep_column(const FieldDesc &f, const V6Geom &g, const double 
   }
 }
 
-// basic update: thread t of nranks*F -> the column of one face point
+// One sweep (dimension g.d) split over its independent parts: thread t of
+// nranks * F * (md+1) -> rank, face point idx (fastest) and part q in
+// [0, md]: q = 0 the low face's add of the lower neighbour's high face,
+// q = md the high face's add of the upper neighbour's low face, else the
+// element pair (q-1, q) along d.  The parts touch disjoint points, so one
+// thread per part gives the column sweep's sums with no chain of dependent
+// loads along the column.
+template <typename I>
+FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
+{
+  const I per = (I)g.F * (I)(g.md + 1);
+  const I r = t / per;
+  const I rem = t - r * per;
+  const I q = rem / (I)g.F;
+  const I idx = rem - q * (I)g.F;
+  const int n = g.n, d = g.d;
+  const V6Point pt = v6_point(g, idx);
+  double *ur = f.u + (long)r * f.R + pt.off;
+  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
+  if (q == 0) {
+    const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
+    if (lo >= 0) *ur = *ur + msg[(long)lo * g.per_rank + g.off + g.F + (long)idx];
+  } else if (q == (I)g.md) {
+    const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
+    if (hi >= 0) {
+      double *p = ur + top + (long)(g.md - 1) * g.sed;
+      *p = *p + msg[(long)hi * g.per_rank + g.off + (long)idx];
+    }
+  } else {
+    const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
+    const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
+    if (!(compute || on_a || on_b)) return;
+    double *p = ur + top + (long)(q - 1) * g.sed;
+    double *pq = p + g.sed - top;
+    const double v = *p + *pq;
+    *p = v;
+    *pq = v;
+  }
+}
+
+// One sweep (dimension g.d), a thread per column: thread t of nranks*F ->
+// the column of one face point (for fields whose sweeps have columns enough
+// to fill the GPU; v6_part_item splits a column over its parts otherwise)
 template <typename I>
 FACES_HD void v6_update_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
 {
