@@ -351,7 +351,7 @@ int faces_status(faces_ctx *c, int *bits)
 int faces_launches_per_share(const faces_ctx *c, int compute)
 {
   if (int rc = check_ctx(c)) return rc;
-  if (c->flags & FACES_V6) return 6;
+  if (c->flags & FACES_V6) return c->nranks == 1 && !(c->flags & FACES_PERIODIC) ? 3 : 6;
   if (c->flags & FACES_V6F) return 4;
   if (compute && seam_step(*c) && c->splan.lean && c->splan.plane_items > 0) return 2;
   if (pack_in_tiles(*c, compute)) return 1;

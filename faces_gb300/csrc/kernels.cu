@@ -552,14 +552,6 @@ __global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
 
 
 template <typename I>
-__global__ void v6_update_kernel(FieldDesc f, V6Geom g, const double *msg, int compute)
-{
-  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
-  if (t >= (I)f.nranks * (I)g.F) return;
-  v6_update_item<I>(f, g, msg, compute, t);
-}
-
-template <typename I>
 __global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int compute, I total)
 {
   const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
@@ -567,26 +559,14 @@ __global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int com
   v6_part_item<I>(f, g, msg, compute, t);
 }
 
-// One sweep's update: a thread per column where the sweep has columns for
-// about four waves of threads (152 SMs x 2048), else a thread per independent
-// part (v6_part_item): the column form keeps each warp walking one element
-// column, the part form puts every warp in the same element layer.  Measured
-// (GB/s): 95x94x93 n = 12 3707 columns, 2818 parts; 40^3 n = 12 3789, 3891;
-// 48^3 n = 8 3216, 3283; 15x14x13 n = 12 1775, 2049; the 3x3x3 grid of 16^3
-// n = 6 ranks 0.180, 0.158 ms per share.
-constexpr long kV6ColumnThreads = 4L * 152 * 2048;
-
-static bool v6_by_columns(const FieldDesc &f, const V6Geom &g) { return (long)f.nranks * g.F >= kV6ColumnThreads; }
-
+// One sweep's update, a thread per independent part in memory order
+// (v6_part_item).  It replaced a thread per column (v6_sweep_column), whose
+// warps each walked a column along d: measured (GB/s) 95x94x93 n = 12 3695
+// -> 4854, 40^3 n = 12 3940 -> 4416, 48^3 n = 8 3278 -> 3374, 15x14x13
+// n = 12 2057 -> 2261, the 3x3x3 grid of 16^3 n = 6 ranks 0.180 -> 0.162 ms.
 static void launch_v6_parts(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, cudaStream_t s)
 {
-  if (v6_by_columns(f, g)) {
-    const long nu = (long)f.nranks * g.F;
-    if (nu + 256 < (1L << 31)) v6_update_kernel<unsigned><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
-    else v6_update_kernel<unsigned long><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, g, msg, compute);
-    return;
-  }
-  const long total = (long)f.nranks * g.F * (g.md + 1);
+  const long total = (long)f.nranks * f.m[0] * f.m[1] * f.m[2] * f.n * f.n;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (total + 256 < (1L << 31)) v6_part_kernel<unsigned><<<blocks, 256, 0, s>>>(f, g, msg, compute, (unsigned)total);
   else v6_part_kernel<unsigned long><<<blocks, 256, 0, s>>>(f, g, msg, compute, (unsigned long)total);
@@ -612,12 +592,18 @@ __global__ void v6_update_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *ms
 
 cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
 {
+  // one non-periodic rank has no neighbour: no face message to pack
+  const bool alone = f.nranks == 1 && !f.periodic;
   for (int d = 2; d >= 0; d--) {
     const V6Geom g = v6_geom(f, d);
     const long np = f.nranks * 2 * g.F;
     // 32-bit index math while every thread index (and the next block's) fits
-    if (np + 256 < (1L << 31)) v6_pack_kernel<unsigned><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
-    else v6_pack_kernel<unsigned long><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+    if (alone) {
+    } else if (np + 256 < (1L << 31)) {
+      v6_pack_kernel<unsigned><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+    } else {
+      v6_pack_kernel<unsigned long><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
+    }
     launch_v6_parts(f, g, msg, compute, s);
   }
   return cudaGetLastError();

@@ -190,55 +190,55 @@ FACES_HD void v6_sweep_column(const FieldDesc &f, const V6Geom &g, const double 
   }
 }
 
-// One sweep (dimension g.d) split over its independent parts: thread t of
-// nranks * F * (md+1) -> rank, face point idx (fastest) and part q in
-// [0, md]: q = 0 the low face's add of the lower neighbour's high face,
-// q = md the high face's add of the upper neighbour's low face, else the
-// element pair (q-1, q) along d.  The parts touch disjoint points, so one
-// thread per part gives the column sweep's sums with no chain of dependent
-// loads along the column.
+// One sweep (dimension g.d) split over its independent parts, in memory
+// order: thread t of nranks * elements * n^2 -> rank, element (jx fastest,
+// then jy, jz) and point (ia, ib) of its face across d (fastest).  The thread
+// sums the element pair (jd, jd+1) along d at that point, and also the low
+// face's add of the lower neighbour's high face when jd = 0 and the high
+// face's add of the upper neighbour's low face when jd = md-1: points no
+// other thread touches, so the column sweep's sums come out with no chain of
+// dependent loads along a column, and concurrent warps work on neighbouring
+// elements (the thread layout of gpu/v-6-messages-basic/Faces.cc:48-104,
+// one block per element there).
 template <typename I>
 FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
 {
-  const I per = (I)g.F * (I)(g.md + 1);
-  const I r = t / per;
-  const I rem = t - r * per;
-  const I q = rem / (I)g.F;
-  const I idx = rem - q * (I)g.F;
   const int n = g.n, d = g.d;
-  const V6Point pt = v6_point(g, idx);
-  double *ur = f.u + (long)r * f.R + pt.off;
-  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
-  if (q == 0) {
+  const I nn = (I)n * (I)n, ne = (I)f.m[0] * (I)f.m[1] * (I)f.m[2];
+  const I face = t % nn;
+  I e = t / nn;
+  const I r = e / ne;
+  e -= r * ne;
+  const int jx = (int)(e % (I)f.m[0]);
+  const I e1 = e / (I)f.m[0];
+  const int jy = (int)(e1 % (I)f.m[1]), jz = (int)(e1 / (I)f.m[1]);
+  const int ia = (int)(face % (I)n), ib = (int)(face / (I)n);
+  // the element's coordinates along a, b (the face's axes) and d
+  const int ja = d == 0 ? jy : jx, jb = d == 2 ? jy : jz, jd = d == 0 ? jx : d == 1 ? jy : jz;
+  const long idx = v6_face_index(g, ia, ib, ja, jb);
+  const long off = ia * g.spa + ib * g.spb + ja * g.sea + jb * g.seb;
+  double *ur = f.u + (long)r * f.R + off;  // this point at coordinate 0 along d, element 0 along d
+  const long top = (long)(n - 1) * g.spd;   // i_d = n - 1 within an element
+  if (jd == 0) {
     const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
-    if (lo >= 0) *ur = *ur + msg[(long)lo * g.per_rank + g.off + g.F + (long)idx];
-  } else if (q == (I)g.md) {
+    if (lo >= 0) *ur = *ur + msg[(long)lo * g.per_rank + g.off + g.F + idx];
+  }
+  if (jd == g.md - 1) {
     const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
     if (hi >= 0) {
       double *p = ur + top + (long)(g.md - 1) * g.sed;
-      *p = *p + msg[(long)hi * g.per_rank + g.off + (long)idx];
+      *p = *p + msg[(long)hi * g.per_rank + g.off + idx];
     }
   } else {
-    const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
-    const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
+    const bool on_a = (ia == 0 && ja == 0) || (ia == n - 1 && ja == g.ma - 1);
+    const bool on_b = (ib == 0 && jb == 0) || (ib == n - 1 && jb == g.mb - 1);
     if (!(compute || on_a || on_b)) return;
-    double *p = ur + top + (long)(q - 1) * g.sed;
+    double *p = ur + top + (long)jd * g.sed;
     double *pq = p + g.sed - top;
     const double v = *p + *pq;
     *p = v;
     *pq = v;
   }
-}
-
-// One sweep (dimension g.d), a thread per column: thread t of nranks*F ->
-// the column of one face point (for fields whose sweeps have columns enough
-// to fill the GPU; v6_part_item splits a column over its parts otherwise)
-template <typename I>
-FACES_HD void v6_update_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
-{
-  const I r = t / (I)g.F;
-  const I idx = t - r * (I)g.F;
-  v6_sweep_column(f, g, msg, compute, (long)r, (long)idx, v6_point(g, idx));
 }
 
 // fused launches B (d = 2) and C (d = 1): the column's sweep, then the

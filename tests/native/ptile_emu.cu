@@ -503,13 +503,9 @@ void launch_both_orders(long nthreads, double *u, long total, double *msg, long 
 
 }  // namespace
 
-// fused: bit 0 the fused form, bit 1 the updates a thread per column
-// (v6_update_item) instead of a thread per part (v6_part_item)
 extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n, int periodic, int fused, int compute,
                           double *u, int nsteps, char *err, int errlen)
 {
-  const bool columns = (fused & 2) != 0;
-  fused &= 1;
   Err e;
   FieldDesc f{};
   f.n = n;
@@ -541,14 +537,8 @@ extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n,
         const V6Geom &g = gs.g[d];
         launch_both_orders(f.nranks * 2 * g.F, fu, total, fm, mtotal,
                            [&](double *uu, double *mm, long t) { v6_pack_item<long>(with(uu), g, mm, t); }, e);
-        if (columns)
-          launch_both_orders(f.nranks * g.F, fu, total, fm, mtotal,
-                             [&](double *uu, double *mm, long t) { v6_update_item<long>(with(uu), g, mm, compute, t); },
-                             e);
-        else
-          launch_both_orders(f.nranks * g.F * (g.md + 1), fu, total, fm, mtotal,
-                             [&](double *uu, double *mm, long t) { v6_part_item<long>(with(uu), g, mm, compute, t); },
-                             e);
+        launch_both_orders((long)f.nranks * f.m[0] * f.m[1] * f.m[2] * n * n, fu, total, fm, mtotal,
+                           [&](double *uu, double *mm, long t) { v6_part_item<long>(with(uu), g, mm, compute, t); }, e);
       }
     } else {
       launch_both_orders(mtotal, fu, total, fm, mtotal,
@@ -559,18 +549,9 @@ extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n,
                              v6_update_pack_item<long>(with(uu), gs, d, mm, compute, t);
                            },
                            e);
-      if (columns)
-        launch_both_orders(f.nranks * gs.g[0].F, fu, total, fm, mtotal,
-                           [&](double *uu, double *mm, long t) {
-                             v6_update_item<long>(with(uu), gs.g[0], mm, compute, t);
-                           },
-                           e);
-      else
-        launch_both_orders(f.nranks * gs.g[0].F * (gs.g[0].md + 1), fu, total, fm, mtotal,
-                           [&](double *uu, double *mm, long t) {
-                             v6_part_item<long>(with(uu), gs.g[0], mm, compute, t);
-                           },
-                           e);
+      launch_both_orders((long)f.nranks * f.m[0] * f.m[1] * f.m[2] * n * n, fu, total, fm, mtotal,
+                         [&](double *uu, double *mm, long t) { v6_part_item<long>(with(uu), gs.g[0], mm, compute, t); },
+                         e);
     }
     if (!guards_intact(field, total) || !guards_intact(msg, mtotal)) e.set("guard cells changed", -1);
   }

@@ -184,7 +184,8 @@ def test_v6_bit_exact(oracle, faces_lib, shape, periodic, fused):
     for init in ("int", "ref"):
         for compute in (True, False):
             f = F.Faces(*shape, periodic=periodic, v6=not fused, v6f=fused)
-            assert f.launches_per_share() == (4 if fused else 6)
+            alone = shape[0] * shape[1] * shape[2] == 1 and not periodic  # no face message to pack
+            assert f.launches_per_share() == (4 if fused else 3 if alone else 6)
             u = f.field()
             f.init_int(u, 5) if init == "int" else f.init_ref(u)
             f.share_n(u, 3, compute)

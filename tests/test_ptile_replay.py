@@ -206,8 +206,7 @@ V6CASES = [
 @pytest.mark.parametrize("case", V6CASES, ids=lambda c: "x".join(map(str, c[:7])) + ("p" if c[7] else "o"))
 @pytest.mark.parametrize("fused", [False, True], ids=["basic", "fused"])
 @pytest.mark.parametrize("compute", [True, False])
-@pytest.mark.parametrize("columns", [False, True], ids=["parts", "columns"])
-def test_v6_replay_matches_oracle(oracle, case, fused, compute, columns):
+def test_v6_replay_matches_oracle(oracle, case, fused, compute):
     """v-6 in both forms, every launch's threads in order and in reverse,
     NaN-filled messages: equals the oracle's v-6 restatement bit for bit."""
     O = oracle
@@ -219,7 +218,7 @@ def test_v6_replay_matches_oracle(oracle, case, fused, compute, columns):
     u0[m] = rng.standard_normal(m.sum())
     u = u0.copy()
     err = ctypes.create_string_buffer(256)
-    rc = v6emu().v6_emulate(*shape, int(periodic), int(fused) | (2 if columns else 0), int(compute),
+    rc = v6emu().v6_emulate(*shape, int(periodic), int(fused), int(compute),
                             u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, err, 256)
     assert rc == 0, err.value.decode()
     exp = O.v6_share(s, u0.copy(), compute, 2)
