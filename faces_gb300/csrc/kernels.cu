@@ -551,25 +551,61 @@ __global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
 }
 
 
-template <typename I>
-__global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int compute, I total)
+// blockIdx.x: position along an element row (element, then face point);
+// blockIdx.y + gridDim.y * blockIdx.z: the row (rank, jz, jy), jy fastest
+template <int N>
+__global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int compute, int per_row)
 {
-  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
-  if (t >= total) return;
-  v6_part_item<I>(f, g, msg, compute, t);
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= per_row) return;
+  const int nn = N > 0 ? N * N : g.n * g.n;
+  const int col = (int)(blockIdx.y + gridDim.y * blockIdx.z);
+  const int jy = col % f.m[1], c2 = col / f.m[1];
+  const int jx = t / nn;
+  v6_part_at<N>(f, g, msg, compute, c2 / f.m[2], jx, jy, c2 % f.m[2], t - jx * nn);
 }
 
 // One sweep's update, a thread per independent part in memory order
-// (v6_part_item).  It replaced a thread per column (v6_sweep_column), whose
+// (v6_part_at).  It replaced a thread per column (v6_sweep_column), whose
 // warps each walked a column along d: measured (GB/s) 95x94x93 n = 12 3695
 // -> 4854, 40^3 n = 12 3940 -> 4416, 48^3 n = 8 3278 -> 3374, 15x14x13
-// n = 12 2057 -> 2261, the 3x3x3 grid of 16^3 n = 6 ranks 0.180 -> 0.162 ms.
-static void launch_v6_parts(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, cudaStream_t s)
+// n = 12 2057 -> 2261, the 3x3x3 grid of 16^3 n = 6 ranks 0.180 -> 0.162 ms;
+// the element from the grid (x: position along a row, y/z: the row) with n
+// a compile-time constant, instead of five run-time divisions per thread:
+// 95x94x93 n = 12 4914 -> 5026 GB/s (one rank, no packs).
+template <int N>
+static cudaError_t launch_v6_parts_n(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, dim3 grid,
+                                     int per_row, cudaStream_t s)
 {
-  const long total = (long)f.nranks * f.m[0] * f.m[1] * f.m[2] * f.n * f.n;
-  const unsigned blocks = (unsigned)((total + 255) / 256);
-  if (total + 256 < (1L << 31)) v6_part_kernel<unsigned><<<blocks, 256, 0, s>>>(f, g, msg, compute, (unsigned)total);
-  else v6_part_kernel<unsigned long><<<blocks, 256, 0, s>>>(f, g, msg, compute, (unsigned long)total);
+  v6_part_kernel<N><<<grid, 256, 0, s>>>(f, g, msg, compute, per_row);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_v6_parts(const FieldDesc &f, const V6Geom &g, const double *msg, int compute,
+                                   cudaStream_t s)
+{
+  const long per_row = (long)f.m[0] * f.n * f.n, cols = (long)f.nranks * f.m[1] * f.m[2];
+  long gy = cols, gz = 1;
+  if (cols > 65535) {
+    gy = f.m[1];
+    gz = cols / f.m[1];
+  }
+  if (per_row + 256 >= (1L << 31) || gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
+  const dim3 grid((unsigned)((per_row + 255) / 256), (unsigned)gy, (unsigned)gz);
+  switch (f.n) {
+    case 2: return launch_v6_parts_n<2>(f, g, msg, compute, grid, (int)per_row, s);
+    case 3: return launch_v6_parts_n<3>(f, g, msg, compute, grid, (int)per_row, s);
+    case 4: return launch_v6_parts_n<4>(f, g, msg, compute, grid, (int)per_row, s);
+    case 5: return launch_v6_parts_n<5>(f, g, msg, compute, grid, (int)per_row, s);
+    case 6: return launch_v6_parts_n<6>(f, g, msg, compute, grid, (int)per_row, s);
+    case 7: return launch_v6_parts_n<7>(f, g, msg, compute, grid, (int)per_row, s);
+    case 8: return launch_v6_parts_n<8>(f, g, msg, compute, grid, (int)per_row, s);
+    case 9: return launch_v6_parts_n<9>(f, g, msg, compute, grid, (int)per_row, s);
+    case 10: return launch_v6_parts_n<10>(f, g, msg, compute, grid, (int)per_row, s);
+    case 11: return launch_v6_parts_n<11>(f, g, msg, compute, grid, (int)per_row, s);
+    case 12: return launch_v6_parts_n<12>(f, g, msg, compute, grid, (int)per_row, s);
+    default: return launch_v6_parts_n<0>(f, g, msg, compute, grid, (int)per_row, s);
+  }
 }
 
 // fused form, launch A
@@ -604,9 +640,10 @@ cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t
     } else {
       v6_pack_kernel<unsigned long><<<(unsigned)((np + 255) / 256), 256, 0, s>>>(f, g, msg);
     }
-    launch_v6_parts(f, g, msg, compute, s);
+    if (cudaError_t e = cudaGetLastError()) return e;
+    if (cudaError_t e = launch_v6_parts(f, g, msg, compute, s)) return e;
   }
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
@@ -628,8 +665,8 @@ cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaSt
     }
   }
   // launch D, the x sweep: a thread per independent part
-  launch_v6_parts(f, gs.g[0], msg, compute, s);
-  return cudaGetLastError();
+  if (cudaError_t e = cudaGetLastError()) return e;
+  return launch_v6_parts(f, gs.g[0], msg, compute, s);
 }
 
 cudaError_t launch_pack(const FieldDesc &f, cudaStream_t s)

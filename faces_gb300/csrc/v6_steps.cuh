@@ -200,19 +200,14 @@ FACES_HD void v6_sweep_column(const FieldDesc &f, const V6Geom &g, const double 
 // dependent loads along a column, and concurrent warps work on neighbouring
 // elements (the thread layout of gpu/v-6-messages-basic/Faces.cc:48-104,
 // one block per element there).
-template <typename I>
-FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
+// the part of element (jx, jy, jz) of rank r at face point `face` (ia
+// fastest); N = n when known at compile time, else 0
+template <int N>
+FACES_HD void v6_part_at(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, int r, int jx, int jy,
+                         int jz, int face)
 {
-  const int n = g.n, d = g.d;
-  const I nn = (I)n * (I)n, ne = (I)f.m[0] * (I)f.m[1] * (I)f.m[2];
-  const I face = t % nn;
-  I e = t / nn;
-  const I r = e / ne;
-  e -= r * ne;
-  const int jx = (int)(e % (I)f.m[0]);
-  const I e1 = e / (I)f.m[0];
-  const int jy = (int)(e1 % (I)f.m[1]), jz = (int)(e1 / (I)f.m[1]);
-  const int ia = (int)(face % (I)n), ib = (int)(face / (I)n);
+  const int n = N > 0 ? N : g.n, d = g.d;
+  const int ia = face % n, ib = face / n;
   // the element's coordinates along a, b (the face's axes) and d
   const int ja = d == 0 ? jy : jx, jb = d == 2 ? jy : jz, jd = d == 0 ? jx : d == 1 ? jy : jz;
   const long idx = v6_face_index(g, ia, ib, ja, jb);
@@ -239,6 +234,19 @@ FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *ms
     *p = v;
     *pq = v;
   }
+}
+
+template <typename I>
+FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
+{
+  const I nn = (I)g.n * (I)g.n, ne = (I)f.m[0] * (I)f.m[1] * (I)f.m[2];
+  const I face = t % nn;
+  I e = t / nn;
+  const I r = e / ne;
+  e -= r * ne;
+  const int jx = (int)(e % (I)f.m[0]);
+  const I e1 = e / (I)f.m[0];
+  v6_part_at<0>(f, g, msg, compute, (int)r, jx, (int)(e1 % (I)f.m[1]), (int)(e1 / (I)f.m[1]), (int)face);
 }
 
 // fused launches B (d = 2) and C (d = 1): the column's sweep, then the
