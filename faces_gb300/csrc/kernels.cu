@@ -566,23 +566,39 @@ __global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int com
 }
 
 // One sweep's update, a thread per independent part in memory order
-// (v6_part_at).  It replaced a thread per column (v6_sweep_column), whose
-// warps each walked a column along d: measured (GB/s) 95x94x93 n = 12 3695
+// (v6_part_at).  It replaced a thread per column along d, whose warps each
+// walked their columns' pairs one by one: measured (GB/s) 95x94x93 n = 12 3695
 // -> 4854, 40^3 n = 12 3940 -> 4416, 48^3 n = 8 3278 -> 3374, 15x14x13
 // n = 12 2057 -> 2261, the 3x3x3 grid of 16^3 n = 6 ranks 0.180 -> 0.162 ms;
 // the element from the grid (x: position along a row, y/z: the row) with n
 // a compile-time constant, instead of five run-time divisions per thread:
 // 95x94x93 n = 12 4914 -> 5026 GB/s (one rank, no packs).
+// fused launches B and C in the part layout (v6_part_pack_at)
+template <int N>
+__global__ void v6_part_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg, int compute, int per_row)
+{
+  const int t = blockIdx.x * 256 + threadIdx.x;
+  if (t >= per_row) return;
+  const int nn = N > 0 ? N * N : f.n * f.n;
+  const int col = (int)(blockIdx.y + gridDim.y * blockIdx.z);
+  const int jy = col % f.m[1], c2 = col / f.m[1];
+  const int jx = t / nn;
+  v6_part_pack_at<N>(f, gs, d, msg, compute, c2 / f.m[2], jx, jy, c2 % f.m[2], t - jx * nn);
+}
+
+// the update of sweep g.d (pack: the fused form's packing update of
+// dimension d, with all three geometries gs)
 template <int N>
 static cudaError_t launch_v6_parts_n(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, dim3 grid,
-                                     int per_row, cudaStream_t s)
+                                     int per_row, cudaStream_t s, const V6Geoms *pack)
 {
-  v6_part_kernel<N><<<grid, 256, 0, s>>>(f, g, msg, compute, per_row);
+  if (pack) v6_part_pack_kernel<N><<<grid, 256, 0, s>>>(f, *pack, g.d, const_cast<double *>(msg), compute, per_row);
+  else v6_part_kernel<N><<<grid, 256, 0, s>>>(f, g, msg, compute, per_row);
   return cudaGetLastError();
 }
 
 static cudaError_t launch_v6_parts(const FieldDesc &f, const V6Geom &g, const double *msg, int compute,
-                                   cudaStream_t s)
+                                   cudaStream_t s, const V6Geoms *pack = nullptr)
 {
   const long per_row = (long)f.m[0] * f.n * f.n, cols = (long)f.nranks * f.m[1] * f.m[2];
   long gy = cols, gz = 1;
@@ -593,18 +609,18 @@ static cudaError_t launch_v6_parts(const FieldDesc &f, const V6Geom &g, const do
   if (per_row + 256 >= (1L << 31) || gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid((unsigned)((per_row + 255) / 256), (unsigned)gy, (unsigned)gz);
   switch (f.n) {
-    case 2: return launch_v6_parts_n<2>(f, g, msg, compute, grid, (int)per_row, s);
-    case 3: return launch_v6_parts_n<3>(f, g, msg, compute, grid, (int)per_row, s);
-    case 4: return launch_v6_parts_n<4>(f, g, msg, compute, grid, (int)per_row, s);
-    case 5: return launch_v6_parts_n<5>(f, g, msg, compute, grid, (int)per_row, s);
-    case 6: return launch_v6_parts_n<6>(f, g, msg, compute, grid, (int)per_row, s);
-    case 7: return launch_v6_parts_n<7>(f, g, msg, compute, grid, (int)per_row, s);
-    case 8: return launch_v6_parts_n<8>(f, g, msg, compute, grid, (int)per_row, s);
-    case 9: return launch_v6_parts_n<9>(f, g, msg, compute, grid, (int)per_row, s);
-    case 10: return launch_v6_parts_n<10>(f, g, msg, compute, grid, (int)per_row, s);
-    case 11: return launch_v6_parts_n<11>(f, g, msg, compute, grid, (int)per_row, s);
-    case 12: return launch_v6_parts_n<12>(f, g, msg, compute, grid, (int)per_row, s);
-    default: return launch_v6_parts_n<0>(f, g, msg, compute, grid, (int)per_row, s);
+    case 2: return launch_v6_parts_n<2>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 3: return launch_v6_parts_n<3>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 4: return launch_v6_parts_n<4>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 5: return launch_v6_parts_n<5>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 6: return launch_v6_parts_n<6>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 7: return launch_v6_parts_n<7>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 8: return launch_v6_parts_n<8>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 9: return launch_v6_parts_n<9>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 10: return launch_v6_parts_n<10>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 11: return launch_v6_parts_n<11>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 12: return launch_v6_parts_n<12>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    default: return launch_v6_parts_n<0>(f, g, msg, compute, grid, (int)per_row, s, pack);
   }
 }
 
@@ -615,15 +631,6 @@ __global__ void v6_early_kernel(FieldDesc f, V6Geoms gs, double *msg)
   const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
   if (t >= (I)f.nranks * (I)gs.g[0].per_rank) return;
   v6_early_item<I>(f, gs, msg, t);
-}
-
-// fused form, launches B (d = 2) and C (d = 1)
-template <typename I>
-__global__ void v6_update_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg, int compute)
-{
-  const I t = blockIdx.x * (I)blockDim.x + threadIdx.x;
-  if (t >= (I)f.nranks * (I)gs.g[d].F) return;
-  v6_update_pack_item<I>(f, gs, d, msg, compute, t);
 }
 
 cudaError_t launch_v6(const FieldDesc &f, double *msg, int compute, cudaStream_t s)
@@ -653,16 +660,15 @@ cudaError_t launch_v6_fused(const FieldDesc &f, double *msg, int compute, cudaSt
   // 32-bit index math while every thread index (and the next block's) fits
   if (na + 256 < (1L << 31)) {
     v6_early_kernel<unsigned><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(f, gs, msg);
-    for (int d = 2; d >= 1; d--) {
-      const long nu = (long)f.nranks * gs.g[d].F;
-      v6_update_pack_kernel<unsigned><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, gs, d, msg, compute);
-    }
   } else {
     v6_early_kernel<unsigned long><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(f, gs, msg);
-    for (int d = 2; d >= 1; d--) {
-      const long nu = (long)f.nranks * gs.g[d].F;
-      v6_update_pack_kernel<unsigned long><<<(unsigned)((nu + 255) / 256), 256, 0, s>>>(f, gs, d, msg, compute);
-    }
+  }
+  // launches B and C, the z and y sweeps with the later sweeps' packs: a
+  // thread per part (measured on the 3x3x3 grid of 16^3 n = 6 ranks: 0.188 ms
+  // per share with a thread per column)
+  for (int d = 2; d >= 1; d--) {
+    if (cudaError_t e = cudaGetLastError()) return e;
+    if (cudaError_t e = launch_v6_parts(f, gs.g[d], msg, compute, s, &gs)) return e;
   }
   // launch D, the x sweep: a thread per independent part
   if (cudaError_t e = cudaGetLastError()) return e;

@@ -10,18 +10,21 @@
 // yfs(ix,iz,jx,jz), xfs(iy,iz,jy,jz)).  Per rank the buffer holds the x, y, z
 // faces, low then high.
 //
+// A sweep runs a thread per independent part (v6_part_at): an element and a
+// point of its face across d, summing the element pair along d there (and
+// the face message adds at the first and last elements).
+//
 // The fused form (v-6 overlap-fusable, gpu/v-6-messages-overlap-fusable/
 // Faces.cc:65-352, there to overlap the MPI transfers with the sweeps): a
-// sweep's thread owns one column along d and finishes every point of it, so
-// it can pack the next sweeps' messages for those points as soon as its own
-// update is done, and points that no later sweep changes can be packed before
-// the first one.  Four launches per share instead of six:
+// sweep's part thread finishes the points it touches, so it can pack the
+// next sweeps' messages for them as soon as its own update is done, and
+// points that no later sweep changes can be packed before the first one.
+// Four launches per share instead of six:
 //   A  every z face; the y-face points with iz interior; the x-face points
 //      with iy and iz interior (no sweep before theirs changes them);
-//   B  the z sweep; a thread whose column is on a y face packs its points
-//      (iz on a seam), one on an x face with iy interior packs its points;
-//   C  the y sweep; a thread whose column is on an x face packs its points
-//      (iy on a seam);
+//   B  the z sweep; a part on a y face packs its points (iz on a seam), one
+//      on an x face with iy interior packs its points;
+//   C  the y sweep; a part on an x face packs its points (iy on a seam);
 //   D  the x sweep.
 // Every message point is packed exactly once, after the last sweep before
 // its own changed it, so the messages and the sums are those of the basic
@@ -157,39 +160,6 @@ FACES_HD void v6_early_item(const FieldDesc &f, const V6Geoms &gs, double *msg, 
   msg[(long)r * pr + g.off + (side ? g.F : 0) + idx] = f.u[(long)r * f.R + v6_face_source(g, p, side)];
 }
 
-// One sweep (dimension g.d) over the column of face point idx of rank r: low
-// face += the lower neighbour's high face, element pairs along d, high face
-// += the upper neighbour's low face; compute = 0: element pairs only where
-// the point is on the subdomain boundary in another dimension.
-FACES_HD void v6_sweep_column(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, long r, long idx,
-                              const V6Point &pt)
-{
-  const int n = g.n, d = g.d;
-  const bool on_a = (pt.ia == 0 && pt.ja == 0) || (pt.ia == n - 1 && pt.ja == g.ma - 1);
-  const bool on_b = (pt.ib == 0 && pt.jb == 0) || (pt.ib == n - 1 && pt.jb == g.mb - 1);
-  const int lo = nbr_of(f, (int)r, dir_index(d == 0 ? -1 : 0, d == 1 ? -1 : 0, d == 2 ? -1 : 0));
-  const int hi = nbr_of(f, (int)r, dir_index(d == 0 ? 1 : 0, d == 1 ? 1 : 0, d == 2 ? 1 : 0));
-  double *ur = f.u + r * f.R + pt.off;
-  const long top = (long)(n - 1) * g.spd;  // i_d = n - 1 within an element
-  if (lo >= 0) {
-    double *p = ur;
-    *p = *p + msg[(long)lo * g.per_rank + g.off + g.F + idx];
-  }
-  if (compute || on_a || on_b) {
-    double *p = ur + top;
-    for (int jd = 0; jd + 1 < g.md; jd++, p += g.sed) {
-      double *q = p + g.sed - top;
-      const double v = *p + *q;
-      *p = v;
-      *q = v;
-    }
-  }
-  if (hi >= 0) {
-    double *p = ur + top + (long)(g.md - 1) * g.sed;
-    *p = *p + msg[(long)hi * g.per_rank + g.off + idx];
-  }
-}
-
 // One sweep (dimension g.d) split over its independent parts, in memory
 // order: thread t of nranks * elements * n^2 -> rank, element (jx fastest,
 // then jy, jz) and point (ia, ib) of its face across d (fastest).  The thread
@@ -236,6 +206,74 @@ FACES_HD void v6_part_at(const FieldDesc &f, const V6Geom &g, const double *msg,
   }
 }
 
+// Fused launches B (d = 2) and C (d = 1) in the part layout: v6_part_at's
+// update, then the messages of the later sweeps for the points it touched --
+// every point with i_d in {0, n-1} belongs to exactly one part: (jd, n-1) to
+// element jd's pair or high add, (jd, 0) to element jd-1's pair or, for
+// jd = 0, the low add.  The z sweep packs a point into the y faces where it
+// lies on one (iy = 0 of jy = 0, iy = n-1 of jy = my-1), and into the x
+// faces where it lies on one with iy interior (the y sweep packs those with
+// iy on a seam); the y sweep packs into the x faces.  The update reads
+// dimension d's faces and the packs write the other dimensions'.
+template <int N>
+FACES_HD void v6_part_pack_at(const FieldDesc &f, const V6Geoms &gs, int d, double *msg, int compute, int r, int jx,
+                              int jy, int jz, int face)
+{
+  const V6Geom &g = gs.g[d];
+  v6_part_at<N>(f, g, msg, compute, r, jx, jy, jz, face);
+  const int n = N > 0 ? N : g.n, nz = n - 1;
+  const int ia = face % n, ib = face / n;
+  const int ja = d == 0 ? jy : jx, jb = d == 2 ? jy : jz, jd = d == 0 ? jx : d == 1 ? jy : jz;
+  const double *ur = f.u + (long)r * f.R + ia * g.spa + ib * g.spb + ja * g.sea + jb * g.seb;
+  const long pr = g.per_rank;
+  auto pack = [&](const V6Geom &h, int side, int pa, int pb, int qa, int qb, const double *src) {
+    msg[(long)r * pr + h.off + (side ? h.F : 0) + v6_face_index(h, pa, pb, qa, qb)] = *src;
+  };
+  // the touched points: (jd, n-1) always, (jd+1, 0) with the pair, (0, 0)
+  // with the low add
+  auto at = [&](int e, int i) { return ur + (long)i * g.spd + (long)e * g.sed; };
+  if (d == 2) {
+    // points (ix, iy, iz; jx, jy, jz) = (ia, ib, iz; ja, jb, e)
+    const int ix = ia, iy = ib;
+    const V6Geom &gy = gs.g[1], &gx = gs.g[0];
+    const int yside = (iy == 0 && jb == 0) ? 0 : (iy == nz && jb == f.m[1] - 1) ? 1 : -1;
+    const int xside = (ix == 0 && ja == 0) ? 0 : (ix == nz && ja == f.m[0] - 1) ? 1 : -1;
+    const bool x_interior_y = iy >= 1 && iy <= n - 2;
+    if (yside < 0 && (xside < 0 || !x_interior_y)) return;
+    auto point = [&](int e, int iz) {
+      const double *src = at(e, iz);
+      if (yside >= 0) pack(gy, yside, ix, iz, ja, e, src);
+      if (xside >= 0 && x_interior_y) pack(gx, xside, iy, iz, jb, e, src);
+    };
+    point(jd, nz);
+    if (jd + 1 < g.md) point(jd + 1, 0);
+    if (jd == 0) point(0, 0);
+  } else if (d == 1) {
+    // points (ix, iy, iz; jx, jy, jz) = (ia, iy, ib; ja, e, jb)
+    const int ix = ia, iz = ib;
+    const V6Geom &gx = gs.g[0];
+    const int xside = (ix == 0 && ja == 0) ? 0 : (ix == nz && ja == f.m[0] - 1) ? 1 : -1;
+    if (xside < 0) return;
+    auto point = [&](int e, int iy) { pack(gx, xside, iy, iz, e, jb, at(e, iy)); };
+    point(jd, nz);
+    if (jd + 1 < g.md) point(jd + 1, 0);
+    if (jd == 0) point(0, 0);
+  }
+}
+
+template <typename I>
+FACES_HD void v6_part_pack_item(const FieldDesc &f, const V6Geoms &gs, int d, double *msg, int compute, I t)
+{
+  const I nn = (I)gs.g[d].n * (I)gs.g[d].n, ne = (I)f.m[0] * (I)f.m[1] * (I)f.m[2];
+  const I face = t % nn;
+  I e = t / nn;
+  const I r = e / ne;
+  e -= r * ne;
+  const int jx = (int)(e % (I)f.m[0]);
+  const I e1 = e / (I)f.m[0];
+  v6_part_pack_at<0>(f, gs, d, msg, compute, (int)r, jx, (int)(e1 % (I)f.m[1]), (int)(e1 / (I)f.m[1]), (int)face);
+}
+
 template <typename I>
 FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, I t)
 {
@@ -247,54 +285,6 @@ FACES_HD void v6_part_item(const FieldDesc &f, const V6Geom &g, const double *ms
   const int jx = (int)(e % (I)f.m[0]);
   const I e1 = e / (I)f.m[0];
   v6_part_at<0>(f, g, msg, compute, (int)r, jx, (int)(e1 % (I)f.m[1]), (int)(e1 / (I)f.m[1]), (int)face);
-}
-
-// fused launches B (d = 2) and C (d = 1): the column's sweep, then the
-// messages of the later sweeps for the column's points (its seam points
-// along d: i_d in {0, n-1}, every j_d).  The sweep reads dimension d's
-// faces and the packs write the other dimensions': disjoint parts of msg.
-template <typename I>
-FACES_HD void v6_update_pack_item(const FieldDesc &f, const V6Geoms &gs, int d, double *msg, int compute, I t)
-{
-  const V6Geom &g = gs.g[d];
-  const I r = t / (I)g.F;
-  const I idx = t - r * (I)g.F;
-  const V6Point pt = v6_point(g, idx);
-  v6_sweep_column(f, g, msg, compute, (long)r, (long)idx, pt);
-  const int n = g.n;
-  const double *ur = f.u + (long)r * f.R;
-  const long pr = g.per_rank;
-  auto pack = [&](const V6Geom &h, int side, int ia, int ib, int ja, int jb, long src) {
-    msg[(long)r * pr + h.off + (side ? h.F : 0) + v6_face_index(h, ia, ib, ja, jb)] = ur[src];
-  };
-  const int nz = n - 1;
-  if (d == 2) {
-    // the thread's column: (ix, iy, jx, jy) = (ia, ib, ja, jb), along z
-    const int ix = pt.ia, iy = pt.ib, jx = pt.ja, jy = pt.jb;
-    const V6Geom &gy = gs.g[1], &gx = gs.g[0];
-    const int yside = (iy == 0 && jy == 0) ? 0 : (iy == nz && jy == f.m[1] - 1) ? 1 : -1;
-    const int xside = (ix == 0 && jx == 0) ? 0 : (ix == nz && jx == f.m[0] - 1) ? 1 : -1;
-    const bool x_interior_y = iy >= 1 && iy <= n - 2;
-    if (yside < 0 && (xside < 0 || !x_interior_y)) return;
-    for (int jz = 0; jz < f.m[2]; jz++)
-      for (int k = 0; k < 2; k++) {
-        const int iz = k ? nz : 0;
-        const long src = pt.off + (long)iz * g.spd + (long)jz * g.sed;
-        if (yside >= 0) pack(gy, yside, ix, iz, jx, jz, src);
-        if (xside >= 0 && x_interior_y) pack(gx, xside, iy, iz, jy, jz, src);
-      }
-  } else if (d == 1) {
-    // the thread's column: (ix, iz, jx, jz) = (ia, ib, ja, jb), along y
-    const int ix = pt.ia, iz = pt.ib, jx = pt.ja, jz = pt.jb;
-    const V6Geom &gx = gs.g[0];
-    const int xside = (ix == 0 && jx == 0) ? 0 : (ix == nz && jx == f.m[0] - 1) ? 1 : -1;
-    if (xside < 0) return;
-    for (int jy = 0; jy < f.m[1]; jy++)
-      for (int k = 0; k < 2; k++) {
-        const int iy = k ? nz : 0;
-        pack(gx, xside, iy, iz, jy, jz, pt.off + (long)iy * g.spd + (long)jy * g.sed);
-      }
-  }
 }
 
 }  // namespace faces

@@ -544,9 +544,9 @@ extern "C" int v6_emulate(int lx, int ly, int lz, int mx, int my, int mz, int n,
       launch_both_orders(mtotal, fu, total, fm, mtotal,
                          [&](double *uu, double *mm, long t) { v6_early_item<long>(with(uu), gs, mm, t); }, e);
       for (int d = 2; d >= 1 && e.ok; d--)
-        launch_both_orders(f.nranks * gs.g[d].F, fu, total, fm, mtotal,
+        launch_both_orders((long)f.nranks * f.m[0] * f.m[1] * f.m[2] * n * n, fu, total, fm, mtotal,
                            [&](double *uu, double *mm, long t) {
-                             v6_update_pack_item<long>(with(uu), gs, d, mm, compute, t);
+                             v6_part_pack_item<long>(with(uu), gs, d, mm, compute, t);
                            },
                            e);
       launch_both_orders((long)f.nranks * f.m[0] * f.m[1] * f.m[2] * n * n, fu, total, fm, mtotal,
