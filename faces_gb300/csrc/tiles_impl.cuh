@@ -412,13 +412,21 @@ inline cudaError_t launch_xtile_fused(const FieldDesc &f, const RowPlan &p, long
   const void *kern = (const void *)xtile_kernel<N, K, kTileStages, OPEN, true>;
   static std::atomic<unsigned long long> configured{0};
   if (cudaError_t e = raise_smem_limit(kern, (int)smem, configured)) return e;
-  int dev = 0, sms = 0, per_sm = 0;
+  // the resident blocks of the whole device, found once per device
+  static std::atomic<long> resident[64];
+  int dev = 0;
   cudaError_t e;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
-      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem)) != cudaSuccess)
-    return e;
-  if (grid > (long)per_sm * sms) grid = (long)per_sm * sms;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  long cap = dev >= 0 && dev < 64 ? resident[dev].load() : 0;
+  if (cap <= 0) {
+    int sms = 0, per_sm = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem)) != cudaSuccess)
+      return e;
+    cap = (long)per_sm * sms;
+    if (dev >= 0 && dev < 64) resident[dev].store(cap);
+  }
+  if (grid > cap) grid = cap;
   if (grid < 1) return cudaErrorCooperativeLaunchTooLarge;
   if ((e = cudaMemsetAsync(pf.counter, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
   FieldDesc fa = f;
