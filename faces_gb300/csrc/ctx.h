@@ -31,10 +31,10 @@ struct faces_ctx {
   double *d_field = nullptr;                // faces_run_host's device copy
   // faces_run_host_many: a second device field, its streams and the events
   // that order uploads, shares and downloads of the two fields
-  double *d_field2 = nullptr;
+  double *d_field2 = nullptr, *d_field3 = nullptr;
   bool pipe_ready = false;
   cudaStream_t s_up = nullptr, s_down = nullptr, s_comp = nullptr;  // uploads, downloads, shares
-  cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  cudaEvent_t ev_up[3] = {}, ev_done[3] = {}, ev_free[3] = {};
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int chunk = 0, tpb = 0, order = -1;
   int sms = 0;       // multiprocessors of the device

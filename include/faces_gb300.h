@@ -155,9 +155,11 @@ int faces_check(faces_ctx *ctx, const double *u, int init, unsigned long long se
 int faces_run_host(faces_ctx *ctx, const double *u_in, double *u_out, int compute, int nshares, void *stream);
 
 /* faces_run_host for njobs independent fields of this context's shape: job j
- * uploads u_in[j], runs nshares shares and downloads to u_out[j].  Two device
- * fields and two copy streams let job j+1's upload and job j-1's download run
- * while job j's shares run on a third stream of the context; all three start
+ * uploads u_in[j], runs nshares shares and downloads to u_out[j].  Three
+ * device fields and two copy streams let job j+1's upload and job j-1's
+ * download run while job j's shares run on a third stream of the context
+ * (the third field: an upload waits for the download of the job three
+ * before it, two jobs' shares of slack); all three streams start
  * after the work already on `stream`, and `stream` ends after them (any
  * stream works, the legacy default one included).  u_out[j] may equal u_in[j], and
  * outputs may repeat across jobs (downloads run in job order); an input may
