@@ -58,6 +58,7 @@ PERIODIC = True
 SEED = 1
 E2E_SHARES = 100  # ni of the configuration (nk=1 nj=1 ni=100)
 E2E_JOBS = 8      # independent jobs per faces_run_host_many call in the e2e leg
+E2E_CALLS = 4     # timed calls (the copies' overlap varies a little from call to call)
 # Every share multiplies a point shared by c copies by c, so integer inputs
 # below 2^20 overflow to +inf after ~330 shares.  As in the reference's own
 # loop (gpu/main.cc:176-184) the field is re-initialized every ni = 100
@@ -315,7 +316,7 @@ def run_faces(args) -> dict | None:
         ins = [hi[j % 2] for j in range(E2E_JOBS)]
         outs = [ho[j % 4] for j in range(E2E_JOBS)]
         f.run_host_many(ins[:2], outs[:2], E2E_SHARES, True, stream)  # warm-up (allocates the device fields)
-        nrep = 4  # calls of E2E_JOBS jobs: the copies' overlap varies a little from call to call
+        nrep = E2E_CALLS
         t0 = time.perf_counter()
         for _ in range(nrep):
             f.run_host_many(ins, outs, E2E_SHARES, True, stream)
