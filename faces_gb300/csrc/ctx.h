@@ -29,8 +29,8 @@ struct faces_ctx {
   int pack_wait_extra = 0;                  // test hook (faces_test_pack_wait)
   long pack_wait_polls = 1L << 22;          // the fused pack's wait bound (about a second)
   double *d_field = nullptr;                // faces_run_host's device copy
-  // faces_run_host_many: a second device field, its streams and the events
-  // that order uploads, shares and downloads of the two fields
+  // faces_run_host_many: two more device fields (jobs rotate over three),
+  // the streams and the events that order uploads, shares and downloads
   double *d_field2 = nullptr, *d_field3 = nullptr;
   bool pipe_ready = false;
   cudaStream_t s_up = nullptr, s_down = nullptr, s_comp = nullptr;  // uploads, downloads, shares
