@@ -83,7 +83,7 @@ def main() -> None:
     ap.add_argument("--argset", choices=list(ARGSETS), help="run this argument set only")
     ap.add_argument("--variant", choices=VARIANTS, help="run this reference build only")
     ap.add_argument("--threads", type=int, choices=THREADS, help="run this MAXTHREADS only")
-    ap.add_argument("--faces-options", choices=["default", "--autotune", "--messages", "--v6", "none"],
+    ap.add_argument("--faces-options", choices=["default", "--autotune", "--messages", "--v6", "--v6f", "--rows", "none"],
                     help="run the faces executable with these options only (none: not at all)")
     args = ap.parse_args()
     if args.argset:
