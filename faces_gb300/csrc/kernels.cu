@@ -552,11 +552,12 @@ __global__ void v6_pack_kernel(FieldDesc f, V6Geom g, double *msg)
 
 
 // blockIdx.x: position along an element row (element, then face point);
-// blockIdx.y + gridDim.y * blockIdx.z: the row (rank, jz, jy), jy fastest
+// blockIdx.y + gridDim.y * blockIdx.z: the row (rank, jz, jy), jy fastest;
+// blockDim.x: v6_part_block
 template <int N>
-__global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int compute, int per_row)
+__global__ void __launch_bounds__(256) v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int compute, int per_row)
 {
-  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= per_row) return;
   const int nn = N > 0 ? N * N : g.n * g.n;
   const int col = (int)(blockIdx.y + gridDim.y * blockIdx.z);
@@ -575,9 +576,10 @@ __global__ void v6_part_kernel(FieldDesc f, V6Geom g, const double *msg, int com
 // 95x94x93 n = 12 4914 -> 5026 GB/s (one rank, no packs).
 // fused launches B and C in the part layout (v6_part_pack_at)
 template <int N>
-__global__ void v6_part_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg, int compute, int per_row)
+__global__ void __launch_bounds__(256) v6_part_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg, int compute,
+                                                           int per_row)
 {
-  const int t = blockIdx.x * 256 + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= per_row) return;
   const int nn = N > 0 ? N * N : f.n * f.n;
   const int col = (int)(blockIdx.y + gridDim.y * blockIdx.z);
@@ -590,11 +592,33 @@ __global__ void v6_part_pack_kernel(FieldDesc f, V6Geoms gs, int d, double *msg,
 // dimension d, with all three geometries gs)
 template <int N>
 static cudaError_t launch_v6_parts_n(const FieldDesc &f, const V6Geom &g, const double *msg, int compute, dim3 grid,
-                                     int per_row, cudaStream_t s, const V6Geoms *pack)
+                                     int block, int per_row, cudaStream_t s, const V6Geoms *pack)
 {
-  if (pack) v6_part_pack_kernel<N><<<grid, 256, 0, s>>>(f, *pack, g.d, const_cast<double *>(msg), compute, per_row);
-  else v6_part_kernel<N><<<grid, 256, 0, s>>>(f, g, msg, compute, per_row);
+  if (pack) v6_part_pack_kernel<N><<<grid, block, 0, s>>>(f, *pack, g.d, const_cast<double *>(msg), compute, per_row);
+  else v6_part_kernel<N><<<grid, block, 0, s>>>(f, g, msg, compute, per_row);
   return cudaGetLastError();
+}
+
+// Threads per block of the part kernels: a row of per_row parts takes whole
+// blocks.  256, unless that leaves more than 1/8 of a row's threads idle;
+// then the size of 128 ... 224 with the fewest idle threads (the larger on a
+// tie).  The C3 grid's rows (16 elements of n = 6: 576 parts) take three
+// blocks of 192, not three of 256 with a quarter of the threads idle
+// (0.161 -> 0.159 ms per share).  Rows that leave less idle keep 256: on
+// 15x14x13 n = 12 (2160 parts, 7 % idle) 128-thread blocks were slower.
+static int v6_part_block(long per_row)
+{
+  int best = 256;
+  long idle = (per_row + 255) / 256 * 256 - per_row;
+  if (idle * 8 <= per_row) return best;
+  for (int b = 224; b >= 128; b -= 32) {
+    const long w = (per_row + b - 1) / b * b - per_row;
+    if (w < idle) {
+      best = b;
+      idle = w;
+    }
+  }
+  return best;
 }
 
 static cudaError_t launch_v6_parts(const FieldDesc &f, const V6Geom &g, const double *msg, int compute,
@@ -607,20 +631,21 @@ static cudaError_t launch_v6_parts(const FieldDesc &f, const V6Geom &g, const do
     gz = cols / f.m[1];
   }
   if (per_row + 256 >= (1L << 31) || gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
-  const dim3 grid((unsigned)((per_row + 255) / 256), (unsigned)gy, (unsigned)gz);
+  const int block = v6_part_block(per_row);
+  const dim3 grid((unsigned)((per_row + block - 1) / block), (unsigned)gy, (unsigned)gz);
   switch (f.n) {
-    case 2: return launch_v6_parts_n<2>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 3: return launch_v6_parts_n<3>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 4: return launch_v6_parts_n<4>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 5: return launch_v6_parts_n<5>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 6: return launch_v6_parts_n<6>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 7: return launch_v6_parts_n<7>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 8: return launch_v6_parts_n<8>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 9: return launch_v6_parts_n<9>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 10: return launch_v6_parts_n<10>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 11: return launch_v6_parts_n<11>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    case 12: return launch_v6_parts_n<12>(f, g, msg, compute, grid, (int)per_row, s, pack);
-    default: return launch_v6_parts_n<0>(f, g, msg, compute, grid, (int)per_row, s, pack);
+    case 2: return launch_v6_parts_n<2>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 3: return launch_v6_parts_n<3>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 4: return launch_v6_parts_n<4>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 5: return launch_v6_parts_n<5>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 6: return launch_v6_parts_n<6>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 7: return launch_v6_parts_n<7>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 8: return launch_v6_parts_n<8>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 9: return launch_v6_parts_n<9>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 10: return launch_v6_parts_n<10>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 11: return launch_v6_parts_n<11>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    case 12: return launch_v6_parts_n<12>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
+    default: return launch_v6_parts_n<0>(f, g, msg, compute, grid, block, (int)per_row, s, pack);
   }
 }
 
