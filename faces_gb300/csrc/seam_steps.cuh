@@ -475,19 +475,6 @@ FACES_HD bool seam_elem_at(const FieldDesc &f, const SeamElem &el, int dx, int d
   return true;
 }
 
-// one face pair along d: this element's copy at `own` + off, the lower
-// neighbour's at lower + off + h (coordinate n-1 along d); lower copy first
-template <class Touch>
-FACES_HD void seam_pair(double *u, long own, long lower, long off, long h, Touch touch)
-{
-  double *p1 = u + own + off, *p0 = u + lower + off + h;
-  touch(p0);
-  touch(p1);
-  const double v = *p0 + *p1;
-  *p0 = v;
-  *p1 = v;
-}
-
 // Edge point at coordinate a of the line along `line` (0: (a, 0, 0), 1:
 // (0, a, 0), 2: (0, 0, a)): a copy for each lower neighbour along its two
 // zero dimensions p < q that exists (2 or 4 copies; 1: nothing to do),
@@ -564,6 +551,55 @@ FACES_HD void seam_corner(const FieldDesc &f, const SeamElem &el, Touch touch)
   }
 }
 
+// The three face pairs of face slot (a, b) of element el (a, b in [1, n-2]):
+// this element's copies (a, b, 0), (a, 0, b), (0, a, b) and the z-, y- and
+// x-lower elements' copies at n-1 along the pair's axis; each sum lower copy
+// first.  The six points are distinct, so every load is issued before any
+// store: their memory latencies overlap instead of following one another.
+template <int N, class Touch>
+FACES_HD void seam_face_pairs(const FieldDesc &f, const SeamElem &el, long own, int a, int b, Touch touch)
+{
+  constexpr long NN = (long)N * N;
+  long lz = 0, ly = 0, lx = 0;
+  const bool hz = seam_elem_at<N>(f, el, 0, 0, -1, lz);
+  const bool hy = seam_elem_at<N>(f, el, 0, -1, 0, ly);
+  const bool hx = seam_elem_at<N>(f, el, -1, 0, 0, lx);
+  const long oz = a + (long)b * N, oy = a + (long)b * NN, ox = (long)a * N + (long)b * NN;
+  double *z1 = f.u + own + oz, *z0 = f.u + lz + oz + (N - 1) * NN;
+  double *y1 = f.u + own + oy, *y0 = f.u + ly + oy + (long)(N - 1) * N;
+  double *x1 = f.u + own + ox, *x0 = f.u + lx + ox + (N - 1);
+  if (hz) {
+    touch(z0);
+    touch(z1);
+  }
+  if (hy) {
+    touch(y0);
+    touch(y1);
+  }
+  if (hx) {
+    touch(x0);
+    touch(x1);
+  }
+  const double vz0 = hz ? *z0 : 0.0, vz1 = hz ? *z1 : 0.0;
+  const double vy0 = hy ? *y0 : 0.0, vy1 = hy ? *y1 : 0.0;
+  const double vx0 = hx ? *x0 : 0.0, vx1 = hx ? *x1 : 0.0;
+  if (hz) {
+    const double v = vz0 + vz1;
+    *z0 = v;
+    *z1 = v;
+  }
+  if (hy) {
+    const double v = vy0 + vy1;
+    *y0 = v;
+    *y1 = v;
+  }
+  if (hx) {
+    const double v = vx0 + vx1;
+    *x0 = v;
+    *x1 = v;
+  }
+}
+
 // lean item t of column col (rank, jz, jy; jy fastest): element t /
 // seam_lean_slots(n) of the column, slot (a, b) in [1, n-2]^2 with a fastest
 // (32-bit decoding: a column holds at most 2^31 items)
@@ -587,10 +623,7 @@ FACES_HD void seam_lean_item(const FieldDesc &f, int col, int t, Touch touch = T
   } else {
     const int bq = s / W;
     const int a = 1 + s - bq * W, b = 1 + bq;
-    long lo;
-    if (seam_elem_at<N>(f, el, 0, 0, -1, lo)) seam_pair(f.u, own, lo, a + (long)b * N, (N - 1) * NN, touch);
-    if (seam_elem_at<N>(f, el, 0, -1, 0, lo)) seam_pair(f.u, own, lo, a + (long)b * NN, (long)(N - 1) * N, touch);
-    if (seam_elem_at<N>(f, el, -1, 0, 0, lo)) seam_pair(f.u, own, lo, (long)a * N + (long)b * NN, N - 1, touch);
+    seam_face_pairs<N>(f, el, own, a, b, touch);
     if (b == 1) {
       seam_edge_point<N>(f, el, own, 0, a, touch);
       seam_edge_point<N>(f, el, own, 1, a, touch);
