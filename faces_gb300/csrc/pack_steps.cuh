@@ -133,20 +133,26 @@ FACES_HD void pack_block(const FieldDesc &f, int by, int bx, int gx, int t, int 
   double *out = f.msg + f.msg_off[rd];
   const double *ur = f.u + base;
   const I nn = (I)(nfree == 2 ? n * n : n), nI = (I)n, mI = (I)m0;
-  for (I pos = part * (I)T + (I)t; pos < sz; pos += parts * (I)T) {
-    long src;
-    if (nfree == 0) {
-      src = 0;
-    } else {
-      const I q = pos % nn, e = pos / nn;
-      if (nfree == 1) {
-        src = (long)q * si0 + (long)e * sj0;
-      } else {
-        src = (long)(q % nI) * si0 + (long)(q / nI) * si1 + (long)(e % mI) * sj0 + (long)(e / mI) * sj1;
-      }
-    }
+  auto source = [&](I pos) -> long {
+    if (nfree == 0) return 0;
+    const I q = pos % nn, e = pos / nn;
+    if (nfree == 1) return (long)q * si0 + (long)e * sj0;
+    return (long)(q % nI) * si0 + (long)(q / nI) * si1 + (long)(e % mI) * sj0 + (long)(e / mI) * sj1;
+  };
+  // the thread's positions pos, pos + S, pos + 2S, ... (S = parts * T), two
+  // at a time with both loads issued before either store, so that their
+  // latencies overlap (a store could alias a later load, so the compiler
+  // keeps them in order otherwise)
+  const I S = parts * (I)T;
+  for (I pos = part * (I)T + (I)t; pos < sz; pos += 2 * S) {
+    const I pos2 = pos + S;
+    const bool two = pos2 < sz;
+    const long src = source(pos), src2 = two ? source(pos2) : 0;
     touch(ur + src);
-    out[pos] = ur[src];
+    if (two) touch(ur + src2);
+    const double v = ur[src], v2 = two ? ur[src2] : 0.0;
+    out[pos] = v;
+    if (two) out[pos2] = v2;
   }
 }
 
