@@ -97,8 +97,8 @@ bool pack_in_tiles(const faces_ctx &c, int compute)
 }
 
 // The default kernel: the seam kernel for direct-mode fields with n >= 11,
-// where it moves more than the tile step (95x94x93 n = 12: 3.85 ms per share
-// against 4.90 open, 4.34 periodic; 15x14x13 n = 12: 0.024 against 0.029;
+// where it moves more than the tile step (95x94x93 n = 12: 3.71 ms per share
+// open against 4.90, 3.85 periodic against 4.34; 15x14x13 n = 12: 0.024 against 0.029;
 // 40^3 n = 11 periodic: 0.259 against 0.276; the tile step wins at n = 10:
 // 48^3 0.313 against 0.353) and the tile step does not reach past n = 12;
 // else the tile step.
@@ -120,7 +120,7 @@ void replan(faces_ctx &c)
     const int fit = seam_blocks_per_sm(c.n);
     // order 1: the lean form, 0: the chunked form; by default the lean form
     // where it gives the GPU four waves of threads (measured: 95x94x93 n = 12
-    // 3.85 ms lean, 4.82 chunked; 15x14x13 n = 12 0.025 lean, 0.023 chunked)
+    // 3.71 ms lean, 4.82 chunked; 15x14x13 n = 12 0.025 lean, 0.023 chunked)
     const long lean_threads = (long)c.nranks * c.m[0] * c.m[1] * c.m[2] * (c.n > 2 ? (c.n - 2) * (c.n - 2) : 1);
     const bool lean = c.order == 1 || (c.order < 0 && lean_threads >= 4L * c.sms * 6 * 256);
     c.splan = make_seam_plan(f, c.chunk, (long)c.sms * (c.tpb > 0 && c.tpb < fit ? c.tpb : fit), lean);
